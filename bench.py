@@ -1,0 +1,403 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 LULESH Lagrange-leapfrog step.
+
+Workload: the Sedov blast at --s 150 --r 21 (3,375,000 hex elements,
+3,442,951 nodes; regions, balance 1 and cost 1 as Domain::Domain builds them),
+the size the reference's headline metric is quoted on. One step = one
+LagrangeLeapFrog cycle (plus the host TimeIncrement before it) over the whole
+mesh. Metric: zone-cycles per second (elements x cycles / seconds).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours (default) prints one JSON line:
+  value          plain double path (LULESH_FP64), state resident in HBM,
+                 device time over K cycles (CUDA events on the library's own
+                 stream, host TimeIncrement and the per-cycle dt readback
+                 included)
+  e2e            the same metric through lulesh_leapfrog, the drop-in for
+                 LagrangeLeapFrog(Domain&): every cycle uploads the state a
+                 step reads from pinned host arrays and downloads everything
+                 it writes; wall clock
+  mixed, graph   the mixed-precision form and the CUDA-graph time loop
+  roofline       dominant kernel vs the measured HBM copy bandwidth, plus its
+                 FP64-pipe roof (the bound that actually applies)
+  cpu_baseline   the CPU oracle (a bit-exact restatement of the reference's
+                 code) on this machine's host cores, bounded sample
+reference: the reference's CPU algorithm (the oracle port) on all host cores,
+same workload, same metric.
+
+Multi-GPU: the step does not shard inside one problem (replicas only); with
+N ranks every rank runs its own s=150 problem and value sums them (weak
+scaling). Rank r uses GPU LOCAL_RANK.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG_DIR = ROOT / "lulesh-task-based-hpx_gb300"
+sys.path.insert(0, str(ROOT / "oracle"))
+
+METRIC = "FOM zone-cycles/s at s=150 (FP64 vs mixed) + batched-ensemble zone-cycles/s"
+UNIT = "zone-cycles/s"
+
+# Algorithmic HBM bytes per unit (element, or node for the node kernel) of each
+# kernel: every array touched once per launch, node fields counted once per
+# node (N_n / N_e ~ 1), neighbour re-reads assumed to hit L2.
+BYTES_PER_UNIT = {
+    "fp64": {"forces": 512, "nodes": 573, "kinematics": 184, "material": 204},
+    "mixed": {"forces": 224, "nodes": 333, "kinematics": 184, "material": 180},
+}
+# Algorithmic double-precision operations per unit (adds, multiplies,
+# divides, square and cube roots each counted once), from counting the
+# reference's arithmetic at s=30 r=11; the material kernel adds 68 per EOS pass.
+FLOPS_PER_UNIT = {"forces": 1809, "nodes": 63, "kinematics": 864, "material_base": 69,
+                  "material_per_rep": 68}
+# Measured on a GB300 of this machine (DFMA throughput probe): 597 G FMA/s.
+FP64_PEAK_TFLOPS = 1.194
+HBM_FALLBACK_GBS = 6800.0
+
+
+def load_package():
+    spec = importlib.util.spec_from_file_location(
+        "lulesh_gb300", PKG_DIR / "__init__.py", submodule_search_locations=[str(PKG_DIR)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["lulesh_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def hbm_peak() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+            os.unlink(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "", 1).isdigit() else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sync():
+    import torch
+
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
+def mean_rep(lul, dom) -> float:
+    import numpy as np
+
+    reg = dom.regNumList - 1
+    nr = dom.nr
+    rep = np.where(reg < nr // 2, 1,
+                   np.where(reg < nr - (nr + 15) // 20, 1 + dom.cost, 10 * (1 + dom.cost)))
+    return float(rep.mean())
+
+
+def roofline(prof: dict, precision: str, ne: int, nn: int, rep_avg: float) -> dict:
+    km = prof["kernel_ms"]
+    cyc = max(prof["cycles"], 1)
+    dom = max(km, key=km.get)
+    units = nn if dom == "nodes" else ne
+    avg_s = km[dom] / cyc / 1e3
+    bytes_launch = BYTES_PER_UNIT[precision][dom] * units
+    peak, kind = hbm_peak()
+    achieved = bytes_launch / avg_s / 1e9
+    if dom == "material":
+        flops = FLOPS_PER_UNIT["material_base"] + FLOPS_PER_UNIT["material_per_rep"] * rep_avg
+    else:
+        flops = FLOPS_PER_UNIT[dom]
+    tflops = flops * units / avg_s / 1e12
+    return {
+        "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+        "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+        "peak_kind": f"{kind} ({'MEASURED_PEAKS.json hbm_gbs' if kind == 'measured' else 'recipe fallback'})",
+        "bytes_per_launch": bytes_launch, "avg_launch_ms": round(km[dom] / cyc, 4),
+        "kernel_share": {k: round(v / max(sum(km.values()), 1e-30), 4) for k, v in km.items()},
+        "fp64_pipe": {"achieved_tflops": round(tflops, 4), "peak_tflops": FP64_PEAK_TFLOPS,
+                      "frac": round(tflops / FP64_PEAK_TFLOPS, 4),
+                      "note": "algorithmic FP64 ops per launch / launch time; peak = measured "
+                              "DFMA rate x 2 (profiles/fp64_pipe_probe.md)"},
+    }
+
+
+def time_device(lul, dom, dev, steps: int, world: int, graph: bool = False) -> dict:
+    barrier(world)
+    sync()
+    dev.profile_begin()
+    if graph:
+        n = dev.run_graph(dom.cycle + steps, 8)
+    else:
+        n = dev.run(dom.cycle + steps)
+    prof = dev.profile_end()
+    sync()
+    barrier(world)
+    if n != steps:
+        raise RuntimeError(f"ran {n} of {steps} cycles (stoptime reached?)")
+    prof["max_ms"] = max_over_ranks(prof["total_ms"], world)
+    return prof
+
+
+def cpu_oracle_rate(s: int, r: int, cycles: int, threads: int) -> tuple[float, float]:
+    import oracle
+
+    o = oracle.Oracle(s, r, 1, 1, threads=threads)
+    o.run(1)  # warm caches and page in the arrays
+    t0 = time.perf_counter()
+    o.run(o.cycle + cycles)
+    dt = time.perf_counter() - t0
+    ne = o.numElem
+    o.close()
+    return ne * cycles / dt, dt
+
+
+def run_ours(args) -> None:
+    rank, world, local = dist_init()
+    lul = load_package()
+    lul.set_device(local)
+    import torch
+
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    s, r, K, W = args.size, args.regions, args.steps, args.warmup
+
+    dom = lul.HostDomain(s, r, 1, 1)
+    ne, nn = dom.numElem, dom.numNode
+    rep_avg = mean_rep(lul, dom)
+    dev = lul.Device(dom, "fp64")
+    dev.run(dom.cycle + W)  # warm-up cycles (untimed)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    prof = time_device(lul, dom, dev, K, world)
+    clk = clocks.stop()
+    value = world * ne * K / (prof["max_ms"] / 1e3)
+    launches = prof["launches"]
+
+    # graph form of the same time loop, same handle, continuing the run
+    gprof = time_device(lul, dom, dev, K, world, graph=True)
+    gvalue = world * ne * K / (gprof["max_ms"] / 1e3)
+
+    # end to end through the drop-in call on pinned host buffers
+    dev.download()
+    dom.pin(True)
+    for _ in range(2):
+        dom.time_increment()
+        dev.leapfrog()
+    barrier(world)
+    sync()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        dom.time_increment()
+        dev.leapfrog()
+    sync()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    barrier(world)
+    e2e_value = world * ne * K / e2e_s
+    h2d = (6 * nn + 5 * ne) * 8
+    d2h = (12 * nn + 11 * ne) * 8 + 16
+    dev.close()
+    dom.close()
+
+    mixed = None
+    if not args.skip_mixed:
+        mdom = lul.HostDomain(s, r, 1, 1)
+        mdev = lul.Device(mdom, "mixed")
+        mdev.run(mdom.cycle + W)
+        mprof = time_device(lul, mdom, mdev, K, world)
+        mvalue = world * ne * K / (mprof["max_ms"] / 1e3)
+        mixed = {"value": round(mvalue, 1), "unit": UNIT, "dtype": "f32 temporaries + f64 state",
+                 "ms_per_step": round(mprof["max_ms"] / K, 4),
+                 "speedup_vs_fp64": round(mvalue / value, 3),
+                 "kernel_ms_per_step": {k: round(v / K, 4) for k, v in mprof["kernel_ms"].items()},
+                 "roofline": roofline(mprof, "mixed", ne, nn, rep_avg)}
+        mdev.close()
+        mdom.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        rate, secs = cpu_oracle_rate(s, r, args.cpu_cycles, threads)
+        cpu = {"value": round(rate, 1), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_cycles} cycles of s={s} r={r} after 1 warm-up cycle "
+                         f"({secs:.1f} s), OpenMP over all host threads"}
+
+    if rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": round(prof["max_ms"] / K, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"Sedov blast --s {s} --r {r} (b=1, c=1), plain double path, "
+                               "host TimeIncrement per cycle",
+                   "elements": ne, "nodes": nn, "mean_eos_rep": round(rep_avg, 3),
+                   "parallelism": "replicas only (one independent problem per GPU)",
+                   "l2": f"no flush: working set {_working_set_gb(ne, nn):.1f} GB per GPU >> 129 MB L2"},
+        "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "how": "lulesh_leapfrog per cycle: upload step inputs from pinned host arrays, "
+                       "run, download every field the step writes; wall clock"},
+        "gpu_launches": launches,
+        "kernel_ms_per_step": {k: round(v / K, 4) for k, v in prof["kernel_ms"].items()},
+        "roofline": roofline(prof, "fp64", ne, nn, rep_avg),
+        "graph": {"value": round(gvalue, 1), "unit": UNIT,
+                  "ms_per_step": round(gprof["max_ms"] / K, 4),
+                  "how": "device TimeIncrement, each cycle replayed from one CUDA graph"},
+        "mixed": mixed,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def _working_set_gb(ne, nn) -> float:
+    return (13 * nn * 8 + nn + 13 * ne * 8 + 25 * ne * 4 + 48 * ne * 8 + 6 * ne * 8) / 1e9
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+
+    s, r, K, W = args.size, args.regions, args.steps, args.warmup
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(s, r, 1, 1, threads=threads)
+    o.run(W)
+    t0 = time.perf_counter()
+    o.run(o.cycle + K)
+    secs = time.perf_counter() - t0
+    ne = o.numElem
+    value = ne * K / secs
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": K, "warmup": W, "ms_per_step": round(1e3 * secs / K, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"Sedov blast --s {s} --r {r} (b=1, c=1)", "elements": ne},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{K} cycles of s={s} r={r} after {W} warm-up cycles; the "
+                                   "reference's algorithm as the bit-exact C oracle (the reference "
+                                   "sources and HPX are not on this machine), OpenMP over all "
+                                   "host threads"},
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--size", type=int, default=150)
+    ap.add_argument("--regions", type=int, default=21)
+    ap.add_argument("--cpu-cycles", type=int, default=20)
+    ap.add_argument("--skip-mixed", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    import oracle
+
+    if not oracle.LIB_PATH.exists():
+        oracle.build(ref=False)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,217 @@
+/* lulesh_gb300.h - C ABI of the GB300-native LULESH Lagrange-leapfrog step.
+ *
+ * Drop-in for the hot path of esa-tu-darmstadt/lulesh-task-based-hpx: the
+ * per-cycle LagrangeLeapFrogWithTasks(Domain&) (reference lulesh.cc:1977-2240)
+ * and the host TimeIncrement (lulesh.cc:182-229) that precedes it in the time
+ * loop of hpx_main (lulesh.cc:2374-2386).
+ *
+ * Conventions
+ *  - Plain C types and pointers only. Every entry point returns a status:
+ *    LULESH_OK or a negative code; LULESH_EVOLUME is the reference's
+ *    VolumeError (lulesh.h:30), the condition on which the reference calls
+ *    exit(VolumeError) (lulesh.cc:821, 908, 1262).
+ *  - A lulesh_dev handle owns one CUDA stream and device copies of every
+ *    Domain array the step touches. Use a handle from one host thread at a
+ *    time. Host arrays stay owned by the caller.
+ *  - All arithmetic of LULESH_FP64 and LULESH_FP64_EXACT is IEEE double, as
+ *    the reference (Real_t = double, lulesh.h:27). LULESH_MIXED runs the
+ *    element force, kinematic and Q-gradient temporaries in float and keeps
+ *    positions, velocities, e, p, q, v and the dt minima in double.
+ */
+#ifndef LULESH_GB300_H
+#define LULESH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define LULESH_OK 0
+#define LULESH_EVOLUME (-1)   /* VolumeError, lulesh.h:30 */
+#define LULESH_EQSTOP (-2)    /* QStopError, lulesh.h:30 (never raised: the reference never checks qstop) */
+#define LULESH_EINVAL (-10)   /* bad argument or size */
+#define LULESH_ECUDA (-11)    /* CUDA runtime error */
+#define LULESH_ENOMEM (-12)   /* device or host allocation failed */
+#define LULESH_ENODEV (-13)   /* no CUDA device */
+#define LULESH_ETIMEOUT (-14) /* a bounded device-side wait gave up */
+
+/* Arithmetic of a device handle. */
+#define LULESH_FP64 0       /* double, FMA contraction allowed (the fast double path) */
+#define LULESH_FP64_EXACT 1 /* double, every operation separately rounded as the reference
+                               source is written; reproduces the CPU oracle bit for bit when
+                               the oracle uses the same cube root (lulesh_cbrt_portable) */
+#define LULESH_MIXED 2      /* float element temporaries, double state (see above) */
+
+/* Physics constants of Domain (lulesh.h:538-560, values lulesh-init.cc:18-36). */
+typedef struct lulesh_params {
+    double e_cut, p_cut, q_cut, v_cut, u_cut;
+    double hgcoef, ss4o3, qstop, monoq_max_slope, monoq_limiter_mult;
+    double qlc_monoq, qqc_monoq, qqc;
+    double eosvmax, eosvmin, pmin, emin, dvovmax, refdens;
+} lulesh_params;
+
+/* Time-control state of Domain (lulesh.h:563-572). */
+typedef struct lulesh_time_state {
+    double time, deltatime, dtcourant, dthydro, dtfixed;
+    double deltatimemultlb, deltatimemultub, dtmax, stoptime;
+    int32_t cycle;
+    int32_t pad_;
+} lulesh_time_state;
+
+/* A view of a host Domain (lulesh.h:130-606): raw pointers to its SoA arrays,
+ * as the Domain accessors *_begin(), nodelist(0), nodeElemCornerList(0) and
+ * regNumList() return them (lulesh.h:281-392). Index arrays are int32
+ * (Index_t, lulesh.h:26), reals double (Real_t, lulesh.h:27). */
+typedef struct lulesh_domain_view {
+    int32_t numElem, numNode;
+    int32_t sizeX;     /* elements along one cube edge (Domain::sizeX) */
+    int32_t numReg;    /* regions (Domain::numReg) */
+    int32_t cost;      /* extra cost of expensive regions (Domain::cost) */
+    int32_t numSymmX, numSymmY, numSymmZ; /* sizes of the symmetry node sets (0 = empty) */
+    /* node-centred, numNode each */
+    double *x, *y, *z, *xd, *yd, *zd, *xdd, *ydd, *zdd, *fx, *fy, *fz;
+    const double* nodalMass;
+    const int32_t *symmX, *symmY, *symmZ;
+    /* element-centred, numElem each unless noted */
+    const int32_t* nodelist; /* 8 * numElem, corners 0..7 of each element */
+    const int32_t *lxim, *lxip, *letam, *letap, *lzetam, *lzetap;
+    const int32_t* elemBC;
+    double *e, *p, *q, *ql, *qq, *v, *vnew, *delv, *vdov, *arealg, *ss;
+    const double *volo, *elemMass;
+    const int32_t* nodeElemStart;      /* numNode + 1 */
+    const int32_t* nodeElemCornerList; /* nodeElemStart[numNode] entries of 8*elem+corner */
+    const int32_t* regNumList;         /* region number 1..numReg of each element */
+    lulesh_params params;
+    lulesh_time_state* time; /* may be NULL except for lulesh_leapfrog */
+} lulesh_domain_view;
+
+/* Field groups for lulesh_dev_upload / lulesh_dev_download. */
+#define LULESH_F_POS 0x001u   /* x y z */
+#define LULESH_F_VEL 0x002u   /* xd yd zd */
+#define LULESH_F_ACC 0x004u   /* xdd ydd zdd */
+#define LULESH_F_FORCE 0x008u /* fx fy fz */
+#define LULESH_F_EPQ 0x010u   /* e p q */
+#define LULESH_F_V 0x020u     /* v */
+#define LULESH_F_QLQQ 0x040u  /* ql qq */
+#define LULESH_F_KIN 0x080u   /* vnew delv vdov arealg */
+#define LULESH_F_SS 0x100u    /* ss */
+/* What one step reads from the mutable state, and everything it writes. */
+#define LULESH_F_STEP_IN (LULESH_F_POS | LULESH_F_VEL | LULESH_F_EPQ | LULESH_F_V | LULESH_F_SS)
+#define LULESH_F_STEP_OUT                                                                \
+    (LULESH_F_POS | LULESH_F_VEL | LULESH_F_ACC | LULESH_F_FORCE | LULESH_F_EPQ |          \
+     LULESH_F_V | LULESH_F_QLQQ | LULESH_F_KIN | LULESH_F_SS)
+#define LULESH_F_ALL 0x1ffu
+
+typedef struct lulesh_dev lulesh_dev;
+typedef struct lulesh_domain lulesh_domain;
+
+/* ---------------- host Domain (replaces Domain::Domain, lulesh-init.cc:10-183) ------- */
+
+/* Builds the Sedov problem of Domain::Domain for an s^3 mesh with nr regions,
+ * load balance `balance` and region cost `cost` (the reference's --s --r --b
+ * --c, lulesh.cc:2421-2432), including the srand(0)/rand() region sets
+ * (lulesh-init.cc:341-445). energy_scale multiplies the deposited energy
+ * (1.0 = the reference); the initial dt follows lulesh-init.cc:181. */
+int lulesh_domain_create(int32_t s, int32_t nr, int32_t balance, int32_t cost, double energy_scale,
+                         lulesh_domain** out);
+/* The view stays valid until lulesh_domain_destroy. */
+lulesh_domain_view* lulesh_domain_get_view(lulesh_domain* d);
+void lulesh_domain_destroy(lulesh_domain* d);
+
+/* TimeIncrement (lulesh.cc:182-229) on a host time state. */
+int lulesh_time_increment(lulesh_time_state* ts);
+
+/* Plane-0 energy symmetry of VerifyAndWriteFinalOutput (lulesh-util.cc:77-103):
+ * out[0] MaxAbsDiff, out[1] TotalAbsDiff, out[2] MaxRelDiff. */
+int lulesh_symmetry(const lulesh_domain_view* v, double out[3]);
+
+/* ---------------- device handle ------------------------------------------------------ */
+
+/* Allocates device mirrors of the Domain arrays the step touches and uploads
+ * all of them (constant topology and the full mutable state). Replaces the
+ * reference's per-cycle malloc/free of temporaries (lulesh.cc:2017-2022,
+ * lulesh.h:203-214): scratch is allocated once here. */
+int lulesh_dev_create(const lulesh_domain_view* host, int32_t precision, lulesh_dev** out);
+void lulesh_dev_destroy(lulesh_dev* dev);
+
+/* Copies field groups host -> device / device -> host (LULESH_F_* masks). */
+int lulesh_dev_upload(lulesh_dev* dev, const lulesh_domain_view* host, uint32_t mask);
+int lulesh_dev_download(lulesh_dev* dev, lulesh_domain_view* host, uint32_t mask);
+
+/* One LagrangeLeapFrog cycle (lulesh.cc:1977-2240) on the device-resident
+ * state with time step `deltatime`; returns the new Courant and hydro
+ * constraints (Domain::dtcourant/dthydro, lulesh.cc:2229-2236). Blocks until
+ * the cycle is done. LULESH_EVOLUME where the reference exits with VolumeError. */
+int lulesh_dev_step(lulesh_dev* dev, double deltatime, double* dtcourant, double* dthydro);
+
+/* The literal drop-in for LagrangeLeapFrogWithTasks(Domain&): uploads the
+ * state a step reads from the host Domain view, runs one cycle with
+ * view->time->deltatime, downloads every field the step writes and stores
+ * dtcourant/dthydro into view->time. */
+int lulesh_leapfrog(lulesh_dev* dev, lulesh_domain_view* host);
+
+/* The time loop of hpx_main (lulesh.cc:2374-2386) on device-resident state:
+ * while (time < stoptime && cycle < max_cycles) { TimeIncrement; step }.
+ * TimeIncrement runs on the host between cycles. *cycles_run counts the
+ * cycles this call ran. */
+int lulesh_dev_run(lulesh_dev* dev, lulesh_time_state* ts, int32_t max_cycles, int32_t* cycles_run);
+
+/* The same time loop with TimeIncrement on the device and each cycle's
+ * kernels replayed from one CUDA graph; the host reads the state back only
+ * every `sync_every` cycles (>= 1). Results equal lulesh_dev_run's. */
+int lulesh_dev_run_graph(lulesh_dev* dev, lulesh_time_state* ts, int32_t max_cycles,
+                         int32_t sync_every, int32_t* cycles_run);
+
+/* Test hooks (no counterpart in the reference; they expose the step's
+ * intermediate arrays so each kernel can be checked on its own). */
+#define LULESH_PHASE_FORCES 0     /* stress + hourglass corner forces */
+#define LULESH_PHASE_NODES 1      /* gather, acceleration, BC, velocity, position */
+#define LULESH_PHASE_KINEMATICS 2 /* kinematics + monotonic-Q gradients */
+#define LULESH_PHASE_MATERIAL 3   /* Q limiter, EOS x rep, sound speed, dt minima */
+int lulesh_dev_phase(lulesh_dev* dev, int32_t phase, double deltatime);
+/* Corner forces of the last force phase, stress + hourglass, element-major
+ * (index 8*elem + corner), double. */
+int lulesh_dev_corner_forces(lulesh_dev* dev, double* fx8, double* fy8, double* fz8);
+/* Monotonic-Q gradients of the last kinematics phase, 6 arrays of numElem:
+ * delv_xi delv_eta delv_zeta delx_xi delx_eta delx_zeta, as double. */
+int lulesh_dev_gradients(lulesh_dev* dev, double* out6);
+/* Element index that raised the last LULESH_EVOLUME (or -1). */
+int32_t lulesh_dev_error_elem(const lulesh_dev* dev);
+/* Number of kernel launches issued by this handle so far. */
+int64_t lulesh_dev_launch_count(const lulesh_dev* dev);
+
+/* Device-side timing (no counterpart in the reference, which wall-clocks
+ * its whole time loop, lulesh.cc:2368-2395). Between begin and end the
+ * handle records CUDA events on its stream: total_ms spans the whole
+ * interval on the device timeline; kernel_ms[k] sums the durations of the
+ * forces, nodes, kinematics and material kernels of lulesh_dev_step cycles
+ * (the graph form contributes to total_ms only). */
+typedef struct lulesh_profile {
+    double total_ms;
+    double kernel_ms[4];
+    int64_t cycles;   /* lulesh_dev_step cycles timed per kernel */
+    int64_t launches; /* kernels launched between begin and end */
+} lulesh_profile;
+int lulesh_dev_profile_begin(lulesh_dev* dev);
+int lulesh_dev_profile_end(lulesh_dev* dev, lulesh_profile* out);
+
+/* Page-locks (pin = 1) or releases (pin = 0) the host arrays of a Domain so
+ * lulesh_leapfrog's per-cycle copies run at full link bandwidth. */
+int lulesh_domain_pin(lulesh_domain* d, int32_t pin);
+
+/* Selects the CUDA device used by handles created afterwards on this thread. */
+int lulesh_set_device(int32_t device);
+
+/* The cube root used by LULESH_FP64_EXACT for the hourglass coefficient
+ * (lulesh.cc:1068 uses cbrt): built from IEEE add/mul/fma/div only, so the
+ * GPU and a CPU build of the same steps round identically. */
+double lulesh_cbrt_portable(double x);
+
+const char* lulesh_strerror(int32_t status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

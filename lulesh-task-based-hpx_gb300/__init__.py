@@ -1,0 +1,294 @@
+"""Python binding of the GB300 LULESH Lagrange-leapfrog step (ctypes over the C ABI).
+
+The library (liblulesh_gb300.so, built in-tree by build.py) is the product:
+hand-written sm_103a kernels behind the C ABI declared in
+include/lulesh_gb300.h. This module only marshals pointers; it has no compute
+of its own and no CPU fallback: if the library is missing or no GPU is
+present, the device calls raise.
+
+    dom = HostDomain(s=30, nr=11)           # Domain::Domain (lulesh-init.cc:10-183)
+    dev = Device(dom, precision="fp64")     # device mirrors of the Domain arrays
+    cycles = dev.run()                       # time loop of hpx_main (lulesh.cc:2374-2386)
+    dev.download()                           # fields back into dom's arrays
+    dom.e[0], dom.symmetry()                 # VerifyAndWriteFinalOutput's checks
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liblulesh_gb300.so"
+
+OK, EVOLUME, EQSTOP, EINVAL, ECUDA, ENOMEM, ENODEV, ETIMEOUT = 0, -1, -2, -10, -11, -12, -13, -14
+PRECISION = {"fp64": 0, "fp64_exact": 1, "mixed": 2}
+
+F_POS, F_VEL, F_ACC, F_FORCE, F_EPQ, F_V, F_QLQQ, F_KIN, F_SS = (1 << k for k in range(9))
+F_STEP_IN = F_POS | F_VEL | F_EPQ | F_V | F_SS
+F_STEP_OUT = F_POS | F_VEL | F_ACC | F_FORCE | F_EPQ | F_V | F_QLQQ | F_KIN | F_SS
+F_ALL = 0x1FF
+
+PHASE_FORCES, PHASE_NODES, PHASE_KINEMATICS, PHASE_MATERIAL = range(4)
+
+NODE_FIELDS = ("x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy", "fz")
+ELEM_FIELDS = ("e", "p", "q", "ql", "qq", "v", "vnew", "delv", "vdov", "arealg", "ss")
+
+
+class LuleshError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {status} ({_strerror(status)})")
+
+
+class Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "e_cut", "p_cut", "q_cut", "v_cut", "u_cut", "hgcoef", "ss4o3", "qstop", "monoq_max_slope",
+        "monoq_limiter_mult", "qlc_monoq", "qqc_monoq", "qqc", "eosvmax", "eosvmin", "pmin", "emin",
+        "dvovmax", "refdens")]
+
+
+class TimeState(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "time", "deltatime", "dtcourant", "dthydro", "dtfixed", "deltatimemultlb", "deltatimemultub",
+        "dtmax", "stoptime")] + [("cycle", C.c_int32), ("pad_", C.c_int32)]
+
+
+_PD, _PI = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+
+
+class Profile(C.Structure):
+    _fields_ = [("total_ms", C.c_double), ("kernel_ms", C.c_double * 4), ("cycles", C.c_int64),
+                ("launches", C.c_int64)]
+
+
+KERNELS = ("forces", "nodes", "kinematics", "material")
+
+
+class DomainView(C.Structure):
+    _fields_ = (
+        [(n, C.c_int32) for n in ("numElem", "numNode", "sizeX", "numReg", "cost", "numSymmX",
+                                   "numSymmY", "numSymmZ")]
+        + [(n, _PD) for n in NODE_FIELDS]
+        + [("nodalMass", _PD), ("symmX", _PI), ("symmY", _PI), ("symmZ", _PI), ("nodelist", _PI)]
+        + [(n, _PI) for n in ("lxim", "lxip", "letam", "letap", "lzetam", "lzetap", "elemBC")]
+        + [(n, _PD) for n in ELEM_FIELDS]
+        + [("volo", _PD), ("elemMass", _PD), ("nodeElemStart", _PI), ("nodeElemCornerList", _PI),
+           ("regNumList", _PI), ("params", Params), ("time", C.POINTER(TimeState))]
+    )
+
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """Loads liblulesh_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is not built: run __graft_entry__.build() or "
+                           f"python {HERE / 'build.py'}")
+    lib = C.CDLL(str(LIB_PATH))
+    vp, i32, i64, u32, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32, C.c_double
+    sig = {
+        "lulesh_domain_create": (i32, [i32, i32, i32, i32, dbl, C.POINTER(vp)]),
+        "lulesh_domain_get_view": (C.POINTER(DomainView), [vp]),
+        "lulesh_domain_destroy": (None, [vp]),
+        "lulesh_time_increment": (i32, [C.POINTER(TimeState)]),
+        "lulesh_symmetry": (i32, [C.POINTER(DomainView), C.POINTER(dbl)]),
+        "lulesh_dev_create": (i32, [C.POINTER(DomainView), i32, C.POINTER(vp)]),
+        "lulesh_dev_destroy": (None, [vp]),
+        "lulesh_dev_upload": (i32, [vp, C.POINTER(DomainView), u32]),
+        "lulesh_dev_download": (i32, [vp, C.POINTER(DomainView), u32]),
+        "lulesh_dev_step": (i32, [vp, dbl, C.POINTER(dbl), C.POINTER(dbl)]),
+        "lulesh_leapfrog": (i32, [vp, C.POINTER(DomainView)]),
+        "lulesh_dev_run": (i32, [vp, C.POINTER(TimeState), i32, C.POINTER(i32)]),
+        "lulesh_dev_run_graph": (i32, [vp, C.POINTER(TimeState), i32, i32, C.POINTER(i32)]),
+        "lulesh_dev_phase": (i32, [vp, i32, dbl]),
+        "lulesh_dev_corner_forces": (i32, [vp, _PD, _PD, _PD]),
+        "lulesh_dev_gradients": (i32, [vp, _PD]),
+        "lulesh_dev_error_elem": (i32, [vp]),
+        "lulesh_dev_launch_count": (i64, [vp]),
+        "lulesh_dev_profile_begin": (i32, [vp]),
+        "lulesh_dev_profile_end": (i32, [vp, C.POINTER(Profile)]),
+        "lulesh_domain_pin": (i32, [vp, i32]),
+        "lulesh_set_device": (i32, [i32]),
+        "lulesh_cbrt_portable": (dbl, [dbl]),
+        "lulesh_strerror": (C.c_char_p, [i32]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _strerror(status: int) -> str:
+    try:
+        return library().lulesh_strerror(status).decode()
+    except Exception:  # library not loadable: plain code
+        return "status"
+
+
+def _check(status: int, what: str) -> None:
+    if status != OK:
+        raise LuleshError(status, what)
+
+
+def _np(ptr, n: int, dtype) -> np.ndarray:
+    return np.ctypeslib.as_array(ptr, shape=(n,)).view(dtype)
+
+
+class HostDomain:
+    """The Sedov problem of Domain::Domain built by the library's host code.
+
+    Field arrays (numpy views onto the library's host vectors): the node fields
+    x y z xd yd zd xdd ydd zdd fx fy fz nodalMass and the element fields
+    e p q ql qq v vnew delv vdov arealg ss volo elemMass, plus the index
+    arrays nodelist nodeElemStart nodeElemCornerList regNumList.
+    """
+
+    def __init__(self, s: int, nr: int = 11, balance: int = 1, cost: int = 1,
+                 energy_scale: float = 1.0):
+        lib = library()
+        h = C.c_void_p()
+        _check(lib.lulesh_domain_create(s, nr, balance, cost, energy_scale, C.byref(h)),
+               "lulesh_domain_create")
+        self._h = h
+        self._lib = lib
+        self.s, self.nr, self.balance, self.cost = s, nr, balance, cost
+        self.view_ptr = lib.lulesh_domain_get_view(h)
+        v = self.view_ptr.contents
+        self.view = v
+        self.numElem, self.numNode = v.numElem, v.numNode
+        for f in NODE_FIELDS:
+            setattr(self, f, _np(getattr(v, f), v.numNode, np.float64))
+        for f in ELEM_FIELDS:
+            setattr(self, f, _np(getattr(v, f), v.numElem, np.float64))
+        self.nodalMass = _np(v.nodalMass, v.numNode, np.float64)
+        self.volo = _np(v.volo, v.numElem, np.float64)
+        self.elemMass = _np(v.elemMass, v.numElem, np.float64)
+        self.nodelist = _np(v.nodelist, 8 * v.numElem, np.int32)
+        self.nodeElemStart = _np(v.nodeElemStart, v.numNode + 1, np.int32)
+        self.nodeElemCornerList = _np(v.nodeElemCornerList, 8 * v.numElem, np.int32)
+        self.regNumList = _np(v.regNumList, v.numElem, np.int32)
+        self.time_state = v.time.contents
+
+    def symmetry(self) -> tuple[float, float, float]:
+        out = (C.c_double * 3)()
+        _check(self._lib.lulesh_symmetry(self.view_ptr, out), "lulesh_symmetry")
+        return out[0], out[1], out[2]
+
+    def time_increment(self) -> None:
+        _check(self._lib.lulesh_time_increment(C.byref(self.time_state)), "lulesh_time_increment")
+
+    @property
+    def cycle(self) -> int:
+        return self.time_state.cycle
+
+    def pin(self, on: bool = True) -> None:
+        """Page-locks the mutable host arrays (fast copies for Device.leapfrog)."""
+        _check(self._lib.lulesh_domain_pin(self._h, 1 if on else 0), "lulesh_domain_pin")
+        self._pinned = on
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            if getattr(self, "_pinned", False):
+                self._lib.lulesh_domain_pin(self._h, 0)
+            self._lib.lulesh_domain_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Device:
+    """Device mirror of a HostDomain; every method runs the sm_103a kernels."""
+
+    def __init__(self, dom: HostDomain, precision: str = "fp64"):
+        lib = library()
+        h = C.c_void_p()
+        _check(lib.lulesh_dev_create(dom.view_ptr, PRECISION[precision], C.byref(h)),
+               "lulesh_dev_create")
+        self._h = h
+        self._lib = lib
+        self.dom = dom
+        self.precision = precision
+
+    def upload(self, mask: int = F_ALL) -> None:
+        _check(self._lib.lulesh_dev_upload(self._h, self.dom.view_ptr, mask), "lulesh_dev_upload")
+
+    def download(self, mask: int = F_ALL) -> None:
+        _check(self._lib.lulesh_dev_download(self._h, self.dom.view_ptr, mask), "lulesh_dev_download")
+
+    def step(self, dt: float) -> tuple[float, float]:
+        dtc, dth = C.c_double(), C.c_double()
+        _check(self._lib.lulesh_dev_step(self._h, dt, C.byref(dtc), C.byref(dth)), "lulesh_dev_step")
+        return dtc.value, dth.value
+
+    def leapfrog(self) -> None:
+        """Drop-in LagrangeLeapFrog on the host Domain (upload, step, download)."""
+        _check(self._lib.lulesh_leapfrog(self._h, self.dom.view_ptr), "lulesh_leapfrog")
+
+    def run(self, max_cycles: int = 9999999) -> int:
+        n = C.c_int32()
+        _check(self._lib.lulesh_dev_run(self._h, C.byref(self.dom.time_state), max_cycles, C.byref(n)),
+               "lulesh_dev_run")
+        return n.value
+
+    def run_graph(self, max_cycles: int = 9999999, sync_every: int = 32) -> int:
+        n = C.c_int32()
+        _check(self._lib.lulesh_dev_run_graph(self._h, C.byref(self.dom.time_state), max_cycles,
+                                              sync_every, C.byref(n)), "lulesh_dev_run_graph")
+        return n.value
+
+    def phase(self, phase: int, dt: float = 0.0) -> None:
+        _check(self._lib.lulesh_dev_phase(self._h, phase, dt), "lulesh_dev_phase")
+
+    def corner_forces(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = 8 * self.dom.numElem
+        out = [np.empty(n, np.float64) for _ in range(3)]
+        ptrs = [o.ctypes.data_as(_PD) for o in out]
+        _check(self._lib.lulesh_dev_corner_forces(self._h, *ptrs), "lulesh_dev_corner_forces")
+        return tuple(out)
+
+    def gradients(self) -> np.ndarray:
+        out = np.empty(6 * self.dom.numElem, np.float64)
+        _check(self._lib.lulesh_dev_gradients(self._h, out.ctypes.data_as(_PD)), "lulesh_dev_gradients")
+        return out.reshape(6, self.dom.numElem)
+
+    def profile_begin(self) -> None:
+        _check(self._lib.lulesh_dev_profile_begin(self._h), "lulesh_dev_profile_begin")
+
+    def profile_end(self) -> dict:
+        p = Profile()
+        _check(self._lib.lulesh_dev_profile_end(self._h, C.byref(p)), "lulesh_dev_profile_end")
+        return {"total_ms": p.total_ms, "kernel_ms": dict(zip(KERNELS, list(p.kernel_ms))),
+                "cycles": p.cycles, "launches": p.launches}
+
+    @property
+    def error_elem(self) -> int:
+        return self._lib.lulesh_dev_error_elem(self._h)
+
+    @property
+    def launches(self) -> int:
+        return self._lib.lulesh_dev_launch_count(self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lulesh_dev_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def cbrt_portable(x: float) -> float:
+    return library().lulesh_cbrt_portable(x)
+
+
+def set_device(device: int) -> None:
+    _check(library().lulesh_set_device(device), "lulesh_set_device")

@@ -1,0 +1,562 @@
+// C ABI of the device path: handle life cycle, host<->device copies, one
+// cycle, and the two forms of the time loop (host TimeIncrement per cycle, or
+// device TimeIncrement with the cycle replayed from a CUDA graph).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "lulesh_dev.h"
+
+namespace {
+
+using lulesh::DevTime;
+using lulesh::Mesh;
+using lulesh::StepResult;
+
+struct Launchers {
+    int (*forces)(const Mesh&, cudaStream_t);
+    int (*nodes)(const Mesh&, double, cudaStream_t);
+    int (*kinematics)(const Mesh&, double, cudaStream_t);
+    int (*material)(const Mesh&, cudaStream_t);
+};
+
+Launchers launchers_for(int precision) {
+    switch (precision) {
+        case LULESH_FP64:
+            return {lulesh::fp64::launch_forces, lulesh::fp64::launch_nodes,
+                    lulesh::fp64::launch_kinematics, lulesh::fp64::launch_material};
+        case LULESH_FP64_EXACT:
+            return {lulesh::fp64x::launch_forces, lulesh::fp64x::launch_nodes,
+                    lulesh::fp64x::launch_kinematics, lulesh::fp64x::launch_material};
+        default:
+            return {lulesh::mixed::launch_forces, lulesh::mixed::launch_nodes,
+                    lulesh::mixed::launch_kinematics, lulesh::mixed::launch_material};
+    }
+}
+
+// Number of EOS evaluations of region index reg (0-based) (lulesh.cc:2156-2170).
+int region_rep(int reg, int numReg, int cost) {
+    if (reg < numReg / 2) return 1;
+    if (reg < (numReg - (numReg + 15) / 20)) return 1 + cost;
+    return 10 * (1 + cost);
+}
+
+// Carves typed arrays out of one device allocation (256-byte aligned).
+struct Arena {
+    size_t used = 0;
+    char* base = nullptr;
+    template <class T>
+    T* take(size_t n) {
+        used = (used + 255) & ~size_t(255);
+        T* p = base ? reinterpret_cast<T*>(base + used) : nullptr;
+        used += n * sizeof(T);
+        return p;
+    }
+};
+
+}  // namespace
+
+struct lulesh_dev {
+    int precision = LULESH_FP64;
+    cudaStream_t stream = nullptr;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    Mesh m{};
+    StepResult* h_result = nullptr;  // pinned
+    DevTime* d_time = nullptr;
+    DevTime* h_time = nullptr;       // pinned
+    cudaGraphExec_t graph = nullptr;
+    int graph_kernels = 0;
+    int64_t launches = 0;
+    int32_t err_elem = -1;
+    Launchers L{};
+    // device-side timing (lulesh_dev_profile_begin/end)
+    bool profiling = false;
+    cudaEvent_t ev[5] = {};
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    double kernel_ms[4] = {0, 0, 0, 0};
+    int64_t prof_cycles = 0, prof_launch0 = 0;
+};
+
+#define CK(call)                                          \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return LULESH_ECUDA;       \
+    } while (0)
+
+namespace {
+
+int validate_view(const lulesh_domain_view* v) {
+    if (!v || v->numElem < 1 || v->numNode < 8 || v->numReg < 1 || v->cost < 0) return LULESH_EINVAL;
+    if ((int64_t)v->numElem * 8 > INT32_MAX) return LULESH_EINVAL;
+    const void* req[] = {v->x, v->y, v->z, v->xd, v->yd, v->zd, v->xdd, v->ydd, v->zdd, v->fx,
+                         v->fy, v->fz, v->nodalMass, v->nodelist, v->lxim, v->lxip, v->letam,
+                         v->letap, v->lzetam, v->lzetap, v->elemBC, v->e, v->p, v->q, v->ql,
+                         v->qq, v->v, v->vnew, v->delv, v->vdov, v->arealg, v->ss, v->volo,
+                         v->elemMass, v->nodeElemStart, v->nodeElemCornerList, v->regNumList};
+    for (const void* p : req)
+        if (!p) return LULESH_EINVAL;
+    const int ne = v->numElem, nn = v->numNode;
+    // every index the kernels dereference must stay inside its array
+    for (int64_t k = 0; k < 8LL * ne; ++k)
+        if (v->nodelist[k] < 0 || v->nodelist[k] >= nn) return LULESH_EINVAL;
+    const int32_t* nb[] = {v->lxim, v->lxip, v->letam, v->letap, v->lzetam, v->lzetap};
+    for (const int32_t* a : nb)
+        for (int i = 0; i < ne; ++i)
+            if (a[i] < 0 || a[i] >= ne) return LULESH_EINVAL;
+    if (v->nodeElemStart[0] != 0) return LULESH_EINVAL;
+    for (int n = 0; n < nn; ++n)
+        if (v->nodeElemStart[n + 1] < v->nodeElemStart[n]) return LULESH_EINVAL;
+    if (v->nodeElemStart[nn] != 8 * ne) return LULESH_EINVAL;
+    for (int64_t k = 0; k < 8LL * ne; ++k)
+        if (v->nodeElemCornerList[k] < 0 || v->nodeElemCornerList[k] >= 8 * ne) return LULESH_EINVAL;
+    for (int i = 0; i < ne; ++i)
+        if (v->regNumList[i] < 1 || v->regNumList[i] > v->numReg) return LULESH_EINVAL;
+    const int32_t* sy[] = {v->symmX, v->symmY, v->symmZ};
+    const int32_t cnt[] = {v->numSymmX, v->numSymmY, v->numSymmZ};
+    for (int a = 0; a < 3; ++a) {
+        if (cnt[a] < 0 || (cnt[a] > 0 && !sy[a])) return LULESH_EINVAL;
+        for (int k = 0; k < cnt[a]; ++k)
+            if (sy[a][k] < 0 || sy[a][k] >= nn) return LULESH_EINVAL;
+    }
+    return LULESH_OK;
+}
+
+// Lays out every device array of the handle in the arena; with base == null
+// it only measures.
+void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
+    Mesh& m = d->m;
+    const bool mixed = d->precision == LULESH_MIXED;
+    for (double** f : {&m.x, &m.y, &m.z, &m.xd, &m.yd, &m.zd, &m.xdd, &m.ydd, &m.zdd, &m.fx, &m.fy,
+                       &m.fz})
+        *f = a.take<double>(nn);
+    m.nodalMass = a.take<double>(nn);
+    m.nodeSymm = a.take<uint8_t>(nn);
+    m.nodelist = a.take<int32_t>(8 * size_t(ne));
+    for (const int32_t** f : {&m.lxim, &m.lxip, &m.letam, &m.letap, &m.lzetam, &m.lzetap, &m.elemBC})
+        *f = a.take<int32_t>(ne);
+    for (double** f : {&m.e, &m.p, &m.q, &m.ql, &m.qq, &m.v, &m.vnew, &m.delv, &m.vdov, &m.arealg,
+                       &m.ss})
+        *f = a.take<double>(ne);
+    m.volo = a.take<double>(ne);
+    m.elemMass = a.take<double>(ne);
+    m.nodeElemStart = a.take<int32_t>(size_t(nn) + 1);
+    m.nodeElemCornerList = a.take<int32_t>(8 * size_t(ne));
+    m.matOrder = a.take<int32_t>(ne);
+    m.elemRep = a.take<int32_t>(ne);
+    if (mixed) {
+        for (float2** f : {&m.pxp, &m.pyp, &m.pzp, &m.vxp, &m.vyp, &m.vzp}) *f = a.take<float2>(nn);
+        for (float** f : {&m.fcx, &m.fcy, &m.fcz}) *f = a.take<float>(8 * size_t(ne));
+        for (float** f : {&m.gvxi, &m.gveta, &m.gvzeta, &m.gxxi, &m.gxeta, &m.gxzeta})
+            *f = a.take<float>(ne);
+    } else {
+        for (double** f : {&m.fsx, &m.fsy, &m.fsz, &m.fhx, &m.fhy, &m.fhz})
+            *f = a.take<double>(8 * size_t(ne));
+        for (double** f : {&m.dvxi, &m.dveta, &m.dvzeta, &m.dxxi, &m.dxeta, &m.dxzeta})
+            *f = a.take<double>(ne);
+    }
+    m.partials = a.take<lulesh::DtPartial>(matGrid);
+    m.result = a.take<StepResult>(1);
+    d->d_time = a.take<DevTime>(1);
+}
+
+struct Copy {
+    void* dev;
+    const void* host;
+    size_t bytes;
+};
+
+// The (device, host) pairs of the field groups in `mask`.
+std::vector<Copy> groups(const lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask) {
+    const Mesh& m = d->m;
+    const size_t nb = sizeof(double) * size_t(m.numNode), eb = sizeof(double) * size_t(m.numElem);
+    std::vector<Copy> c;
+    if (mask & LULESH_F_POS) c.insert(c.end(), {{m.x, v->x, nb}, {m.y, v->y, nb}, {m.z, v->z, nb}});
+    if (mask & LULESH_F_VEL) c.insert(c.end(), {{m.xd, v->xd, nb}, {m.yd, v->yd, nb}, {m.zd, v->zd, nb}});
+    if (mask & LULESH_F_ACC)
+        c.insert(c.end(), {{m.xdd, v->xdd, nb}, {m.ydd, v->ydd, nb}, {m.zdd, v->zdd, nb}});
+    if (mask & LULESH_F_FORCE)
+        c.insert(c.end(), {{m.fx, v->fx, nb}, {m.fy, v->fy, nb}, {m.fz, v->fz, nb}});
+    if (mask & LULESH_F_EPQ) c.insert(c.end(), {{m.e, v->e, eb}, {m.p, v->p, eb}, {m.q, v->q, eb}});
+    if (mask & LULESH_F_V) c.push_back({m.v, v->v, eb});
+    if (mask & LULESH_F_QLQQ) c.insert(c.end(), {{m.ql, v->ql, eb}, {m.qq, v->qq, eb}});
+    if (mask & LULESH_F_KIN)
+        c.insert(c.end(), {{m.vnew, v->vnew, eb}, {m.delv, v->delv, eb}, {m.vdov, v->vdov, eb},
+                           {m.arealg, v->arealg, eb}});
+    if (mask & LULESH_F_SS) c.push_back({m.ss, v->ss, eb});
+    return c;
+}
+
+int run_cycle(lulesh_dev* d, double dt) {
+    const Mesh& m = d->m;
+    const bool prof = d->profiling;
+    CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
+    if (prof) CK(cudaEventRecord(d->ev[0], d->stream));
+    d->launches += d->L.forces(m, d->stream);
+    if (prof) CK(cudaEventRecord(d->ev[1], d->stream));
+    d->launches += d->L.nodes(m, dt, d->stream);
+    if (prof) CK(cudaEventRecord(d->ev[2], d->stream));
+    d->launches += d->L.kinematics(m, dt, d->stream);
+    if (prof) CK(cudaEventRecord(d->ev[3], d->stream));
+    d->launches += d->L.material(m, d->stream);
+    if (prof) CK(cudaEventRecord(d->ev[4], d->stream));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(d->h_result, m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
+    CK(cudaStreamSynchronize(d->stream));
+    if (prof) {
+        for (int k = 0; k < 4; ++k) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, d->ev[k], d->ev[k + 1]));
+            d->kernel_ms[k] += ms;
+        }
+        ++d->prof_cycles;
+    }
+    if (d->h_result->err != 0) {
+        d->err_elem = d->h_result->err_elem;
+        return d->h_result->err;
+    }
+    return LULESH_OK;
+}
+
+int build_graph(lulesh_dev* d) {
+    if (d->graph) return LULESH_OK;
+    Mesh gm = d->m;
+    gm.dtime = d->d_time;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+    int k = 0;
+    k += lulesh::launch_time_increment(d->d_time, gm.result, d->stream);
+    k += d->L.forces(gm, d->stream);
+    k += d->L.nodes(gm, 0.0, d->stream);
+    k += d->L.kinematics(gm, 0.0, d->stream);
+    k += d->L.material(gm, d->stream);
+    k += lulesh::launch_time_finish(d->d_time, gm.result, d->stream);
+    cudaError_t ce = cudaStreamEndCapture(d->stream, &g);
+    if (ce != cudaSuccess) return LULESH_ECUDA;
+    ce = cudaGraphInstantiate(&d->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+        d->graph = nullptr;
+        return LULESH_ECUDA;
+    }
+    d->graph_kernels = k;
+    return LULESH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev** out) {
+    if (!out) return LULESH_EINVAL;
+    *out = nullptr;
+    if (precision != LULESH_FP64 && precision != LULESH_FP64_EXACT && precision != LULESH_MIXED)
+        return LULESH_EINVAL;
+    int st = validate_view(v);
+    if (st != LULESH_OK) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LULESH_ENODEV;
+    int dev_id = 0, sms = 0;
+    CK(cudaGetDevice(&dev_id));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+
+    const int ne = v->numElem, nn = v->numNode;
+    // derived host arrays: per-node symmetry bits, per-element EOS repeat
+    // count and the repeat-count grouping of the material kernel
+    std::vector<uint8_t> symm(nn, 0);
+    for (int k = 0; k < v->numSymmX; ++k) symm[v->symmX[k]] |= 1;
+    for (int k = 0; k < v->numSymmY; ++k) symm[v->symmY[k]] |= 2;
+    for (int k = 0; k < v->numSymmZ; ++k) symm[v->symmZ[k]] |= 4;
+    std::vector<int32_t> rep(ne), order(ne);
+    for (int i = 0; i < ne; ++i) rep[i] = region_rep(v->regNumList[i] - 1, v->numReg, v->cost);
+    for (int i = 0; i < ne; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rep[a] > rep[b]; });
+
+    lulesh_dev* d = new (std::nothrow) lulesh_dev;
+    if (!d) return LULESH_ENOMEM;
+    d->precision = precision;
+    d->L = launchers_for(precision);
+    const int matGrid = std::max(1, std::min(lulesh::blocks_for(ne, lulesh::kMatBlock), sms * 8));
+    Arena measure;
+    layout(d, measure, ne, nn, matGrid);
+    d->arena_bytes = measure.used;
+    auto fail = [&](int code) {
+        lulesh_dev_destroy(d);
+        return code;
+    };
+    if (cudaMalloc(&d->arena, d->arena_bytes) != cudaSuccess) return fail(LULESH_ENOMEM);
+    Arena carve;
+    carve.base = static_cast<char*>(d->arena);
+    layout(d, carve, ne, nn, matGrid);
+    Mesh& m = d->m;
+    m.numElem = ne;
+    m.numNode = nn;
+    m.matGrid = matGrid;
+    m.prm = v->params;
+    m.dtime = nullptr;
+    if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(LULESH_ECUDA);
+    if (cudaMallocHost(&d->h_result, sizeof(StepResult)) != cudaSuccess) return fail(LULESH_ENOMEM);
+    if (cudaMallocHost(&d->h_time, sizeof(DevTime)) != cudaSuccess) return fail(LULESH_ENOMEM);
+
+    const size_t eb = sizeof(int32_t) * size_t(ne);
+    const Copy consts[] = {
+        {const_cast<double*>(m.nodalMass), v->nodalMass, sizeof(double) * size_t(nn)},
+        {const_cast<uint8_t*>(m.nodeSymm), symm.data(), size_t(nn)},
+        {const_cast<int32_t*>(m.nodelist), v->nodelist, 8 * eb},
+        {const_cast<int32_t*>(m.lxim), v->lxim, eb},
+        {const_cast<int32_t*>(m.lxip), v->lxip, eb},
+        {const_cast<int32_t*>(m.letam), v->letam, eb},
+        {const_cast<int32_t*>(m.letap), v->letap, eb},
+        {const_cast<int32_t*>(m.lzetam), v->lzetam, eb},
+        {const_cast<int32_t*>(m.lzetap), v->lzetap, eb},
+        {const_cast<int32_t*>(m.elemBC), v->elemBC, eb},
+        {const_cast<double*>(m.volo), v->volo, sizeof(double) * size_t(ne)},
+        {const_cast<double*>(m.elemMass), v->elemMass, sizeof(double) * size_t(ne)},
+        {const_cast<int32_t*>(m.nodeElemStart), v->nodeElemStart, sizeof(int32_t) * (size_t(nn) + 1)},
+        {const_cast<int32_t*>(m.nodeElemCornerList), v->nodeElemCornerList, 8 * eb},
+        {const_cast<int32_t*>(m.matOrder), order.data(), eb},
+        {const_cast<int32_t*>(m.elemRep), rep.data(), eb},
+    };
+    for (const Copy& c : consts)
+        if (cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, d->stream) != cudaSuccess)
+            return fail(LULESH_ECUDA);
+    if (cudaMemsetAsync(m.result, 0, sizeof(StepResult), d->stream) != cudaSuccess)
+        return fail(LULESH_ECUDA);
+    // the copies above read pageable host vectors that die with this scope
+    if (cudaStreamSynchronize(d->stream) != cudaSuccess) return fail(LULESH_ECUDA);
+    st = lulesh_dev_upload(d, v, LULESH_F_ALL);
+    if (st != LULESH_OK) return fail(st);
+    *out = d;
+    return LULESH_OK;
+}
+
+void lulesh_dev_destroy(lulesh_dev* d) {
+    if (!d) return;
+    if (d->stream) cudaStreamSynchronize(d->stream);
+    for (cudaEvent_t e : d->ev)
+        if (e) cudaEventDestroy(e);
+    if (d->ev_begin) cudaEventDestroy(d->ev_begin);
+    if (d->ev_end) cudaEventDestroy(d->ev_end);
+    if (d->graph) cudaGraphExecDestroy(d->graph);
+    if (d->arena) cudaFree(d->arena);
+    if (d->h_result) cudaFreeHost(d->h_result);
+    if (d->h_time) cudaFreeHost(d->h_time);
+    if (d->stream) cudaStreamDestroy(d->stream);
+    delete d;
+}
+
+int lulesh_dev_upload(lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask) {
+    if (!d || !v || v->numElem != d->m.numElem || v->numNode != d->m.numNode) return LULESH_EINVAL;
+    for (const Copy& c : groups(d, v, mask)) {
+        if (!c.host) return LULESH_EINVAL;
+        CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, d->stream));
+    }
+    if (d->precision == LULESH_MIXED && (mask & (LULESH_F_POS | LULESH_F_VEL))) {
+        d->launches += lulesh::mixed::launch_mirror(d->m, d->stream);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(d->stream));
+    return LULESH_OK;
+}
+
+int lulesh_dev_download(lulesh_dev* d, lulesh_domain_view* v, uint32_t mask) {
+    if (!d || !v || v->numElem != d->m.numElem || v->numNode != d->m.numNode) return LULESH_EINVAL;
+    for (const Copy& c : groups(d, v, mask)) {
+        if (!c.host) return LULESH_EINVAL;
+        CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->stream));
+    }
+    CK(cudaStreamSynchronize(d->stream));
+    return LULESH_OK;
+}
+
+int lulesh_dev_step(lulesh_dev* d, double dt, double* dtcourant, double* dthydro) {
+    if (!d || !(dt > 0.0)) return LULESH_EINVAL;
+    const int st = run_cycle(d, dt);
+    if (st != LULESH_OK) return st;
+    if (dtcourant) *dtcourant = d->h_result->dtcourant;
+    if (dthydro) *dthydro = d->h_result->dthydro;
+    return LULESH_OK;
+}
+
+int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
+    if (!d || !v || !v->time) return LULESH_EINVAL;
+    int st = lulesh_dev_upload(d, v, LULESH_F_STEP_IN);
+    if (st != LULESH_OK) return st;
+    st = lulesh_dev_step(d, v->time->deltatime, &v->time->dtcourant, &v->time->dthydro);
+    if (st != LULESH_OK) return st;
+    return lulesh_dev_download(d, v, LULESH_F_STEP_OUT);
+}
+
+int lulesh_dev_run(lulesh_dev* d, lulesh_time_state* ts, int32_t max_cycles, int32_t* cycles_run) {
+    if (!d || !ts) return LULESH_EINVAL;
+    int32_t n = 0;
+    int st = LULESH_OK;
+    while (ts->time < ts->stoptime && ts->cycle < max_cycles) {
+        lulesh_time_increment(ts);
+        st = lulesh_dev_step(d, ts->deltatime, &ts->dtcourant, &ts->dthydro);
+        if (st != LULESH_OK) break;
+        ++n;
+    }
+    if (cycles_run) *cycles_run = n;
+    return st;
+}
+
+int lulesh_dev_run_graph(lulesh_dev* d, lulesh_time_state* ts, int32_t max_cycles,
+                         int32_t sync_every, int32_t* cycles_run) {
+    if (!d || !ts || sync_every < 1) return LULESH_EINVAL;
+    int st = build_graph(d);
+    if (st != LULESH_OK) return st;
+    DevTime& h = *d->h_time;
+    h = DevTime{};
+    h.time = ts->time;
+    h.deltatime = ts->deltatime;
+    h.dtcourant = ts->dtcourant;
+    h.dthydro = ts->dthydro;
+    h.dtfixed = ts->dtfixed;
+    h.deltatimemultlb = ts->deltatimemultlb;
+    h.deltatimemultub = ts->deltatimemultub;
+    h.dtmax = ts->dtmax;
+    h.stoptime = ts->stoptime;
+    h.cycle = ts->cycle;
+    h.max_cycles = max_cycles;
+    h.active = 1;
+    const int32_t start = ts->cycle;
+    CK(cudaMemsetAsync(d->m.result, 0, sizeof(StepResult), d->stream));
+    CK(cudaMemcpyAsync(d->d_time, d->h_time, sizeof(DevTime), cudaMemcpyHostToDevice, d->stream));
+    for (;;) {
+        for (int k = 0; k < sync_every; ++k) {
+            CK(cudaGraphLaunch(d->graph, d->stream));
+            d->launches += d->graph_kernels;
+        }
+        CK(cudaMemcpyAsync(d->h_time, d->d_time, sizeof(DevTime), cudaMemcpyDeviceToHost, d->stream));
+        CK(cudaMemcpyAsync(d->h_result, d->m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
+        CK(cudaStreamSynchronize(d->stream));
+        if (!h.active) break;
+    }
+    ts->time = h.time;
+    ts->deltatime = h.deltatime;
+    ts->dtcourant = h.dtcourant;
+    ts->dthydro = h.dthydro;
+    ts->cycle = h.cycle;
+    if (cycles_run) *cycles_run = h.cycle - start;
+    if (d->h_result->err != 0) {
+        d->err_elem = d->h_result->err_elem;
+        return d->h_result->err;
+    }
+    return LULESH_OK;
+}
+
+int lulesh_dev_phase(lulesh_dev* d, int32_t phase, double dt) {
+    if (!d) return LULESH_EINVAL;
+    const Mesh& m = d->m;
+    CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
+    switch (phase) {
+        case LULESH_PHASE_FORCES: d->launches += d->L.forces(m, d->stream); break;
+        case LULESH_PHASE_NODES: d->launches += d->L.nodes(m, dt, d->stream); break;
+        case LULESH_PHASE_KINEMATICS: d->launches += d->L.kinematics(m, dt, d->stream); break;
+        case LULESH_PHASE_MATERIAL: d->launches += d->L.material(m, d->stream); break;
+        default: return LULESH_EINVAL;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(d->h_result, m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
+    CK(cudaStreamSynchronize(d->stream));
+    if (d->h_result->err != 0) {
+        d->err_elem = d->h_result->err_elem;
+        return d->h_result->err;
+    }
+    return LULESH_OK;
+}
+
+int lulesh_dev_corner_forces(lulesh_dev* d, double* fx8, double* fy8, double* fz8) {
+    if (!d || !fx8 || !fy8 || !fz8) return LULESH_EINVAL;
+    const Mesh& m = d->m;
+    const size_t N = size_t(m.numElem), n8 = 8 * N;
+    double* outs[3] = {fx8, fy8, fz8};
+    if (d->precision == LULESH_MIXED) {
+        std::vector<float> buf(n8);
+        const float* src[3] = {m.fcx, m.fcy, m.fcz};
+        for (int a = 0; a < 3; ++a) {
+            CK(cudaMemcpy(buf.data(), src[a], n8 * sizeof(float), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < N; ++i)
+                for (int k = 0; k < 8; ++k) outs[a][8 * i + k] = double(buf[k * N + i]);
+        }
+        return LULESH_OK;
+    }
+    std::vector<double> s(n8), h(n8);
+    const double* ss[3] = {m.fsx, m.fsy, m.fsz};
+    const double* hh[3] = {m.fhx, m.fhy, m.fhz};
+    for (int a = 0; a < 3; ++a) {
+        CK(cudaMemcpy(s.data(), ss[a], n8 * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(h.data(), hh[a], n8 * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < N; ++i)
+            for (int k = 0; k < 8; ++k) outs[a][8 * i + k] = s[k * N + i] + h[k * N + i];
+    }
+    return LULESH_OK;
+}
+
+int lulesh_dev_gradients(lulesh_dev* d, double* out6) {
+    if (!d || !out6) return LULESH_EINVAL;
+    const Mesh& m = d->m;
+    const size_t N = size_t(m.numElem);
+    if (d->precision == LULESH_MIXED) {
+        std::vector<float> buf(N);
+        const float* src[6] = {m.gvxi, m.gveta, m.gvzeta, m.gxxi, m.gxeta, m.gxzeta};
+        for (int a = 0; a < 6; ++a) {
+            CK(cudaMemcpy(buf.data(), src[a], N * sizeof(float), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < N; ++i) out6[a * N + i] = double(buf[i]);
+        }
+        return LULESH_OK;
+    }
+    const double* src[6] = {m.dvxi, m.dveta, m.dvzeta, m.dxxi, m.dxeta, m.dxzeta};
+    for (int a = 0; a < 6; ++a)
+        CK(cudaMemcpy(out6 + a * N, src[a], N * sizeof(double), cudaMemcpyDeviceToHost));
+    return LULESH_OK;
+}
+
+int lulesh_dev_profile_begin(lulesh_dev* d) {
+    if (!d) return LULESH_EINVAL;
+    if (!d->ev_begin) {
+        for (cudaEvent_t& e : d->ev) CK(cudaEventCreate(&e));
+        CK(cudaEventCreate(&d->ev_begin));
+        CK(cudaEventCreate(&d->ev_end));
+    }
+    for (double& k : d->kernel_ms) k = 0.0;
+    d->prof_cycles = 0;
+    d->prof_launch0 = d->launches;
+    d->profiling = true;
+    CK(cudaEventRecord(d->ev_begin, d->stream));
+    return LULESH_OK;
+}
+
+int lulesh_dev_profile_end(lulesh_dev* d, lulesh_profile* out) {
+    if (!d || !out || !d->profiling) return LULESH_EINVAL;
+    d->profiling = false;
+    CK(cudaEventRecord(d->ev_end, d->stream));
+    CK(cudaEventSynchronize(d->ev_end));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, d->ev_begin, d->ev_end));
+    out->total_ms = ms;
+    for (int k = 0; k < 4; ++k) out->kernel_ms[k] = d->kernel_ms[k];
+    out->cycles = d->prof_cycles;
+    out->launches = d->launches - d->prof_launch0;
+    return LULESH_OK;
+}
+
+int lulesh_set_device(int32_t device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return LULESH_ENODEV;
+    if (device < 0 || device >= n) return LULESH_EINVAL;
+    CK(cudaSetDevice(device));
+    return LULESH_OK;
+}
+
+int32_t lulesh_dev_error_elem(const lulesh_dev* d) { return d ? d->err_elem : -1; }
+
+int64_t lulesh_dev_launch_count(const lulesh_dev* d) { return d ? d->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,205 @@
+// Double-precision kernels of the Lagrange-leapfrog step.
+//
+// This header is compiled twice:
+//   fp64_fast.cu   LULESH_VARIANT=fp64,  LULESH_EXACT=0, FMA contraction on
+//   fp64_exact.cu  LULESH_VARIANT=fp64x, LULESH_EXACT=1, nvcc --fmad=false
+// With the reference's operand order kept in step_math.cuh, the exact
+// variant rounds every operation as the reference does and matches the CPU
+// oracle bit for bit (the oracle then uses the same portable cube root); the
+// fast variant lets nvcc fuse multiply-adds, which moves results by a few
+// ulps and saves FP64-pipe instructions.
+//
+// One cycle = four kernels:
+//   k_forces      element: stress + FB hourglass corner forces   (lulesh.cc:787-1113)
+//   k_nodes       node: CSR gather, a = f/m, symmetry BC, v, x    (lulesh.cc:838-862, 1115-1158, 566-588)
+//   k_kinematics  element: volume, arealg, vdov, v <- vnew, Q gradients (lulesh.cc:1169-1418)
+//   k_material    element in repeat-count order: Q limiter, EOS x rep, sound
+//                 speed, save, Courant/hydro dt minima          (lulesh.cc:1420-1974)
+#pragma once
+
+#include "step_math.cuh"
+
+namespace lulesh {
+namespace LULESH_VARIANT {
+
+__device__ __forceinline__ double cube_root(double x) {
+#if LULESH_EXACT
+    return cbrt_portable(x);
+#else
+    return cbrt(x);
+#endif
+}
+
+// Stress and hourglass corner forces of one element per thread, stored
+// separately (corner-major) so that the node gather adds them in the
+// reference's order (lulesh.cc:849-856).
+__global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m) {
+    if (m.dtime && !m.dtime->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.numElem) return;
+    const size_t N = (size_t)m.numElem;
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    double x[8], y[8], z[8];
+    gather8(m.x, nl, x);
+    gather8(m.y, nl, y);
+    gather8(m.z, nl, z);
+
+    // stress (InitIntegrateStressForElemsTask, lulesh.cc:787-836)
+    {
+        const double sig = -LD(m.p + i) - LD(m.q + i);
+        if (jac_det(jacobian(x, y, z)) == 0) raise_error(m.result, i, PHASE_FORCES);
+        double nx[8], ny[8], nz[8];
+        node_normals(nx, ny, nz, x, y, z);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            m.fsx[k * N + i] = -(sig * nx[k]);
+            m.fsy[k * N + i] = -(sig * ny[k]);
+            m.fsz[k * N + i] = -(sig * nz[k]);
+        }
+    }
+
+    // hourglass (CalcHourglassForElemsTask, lulesh.cc:864-1113)
+    const double determ = LD(m.volo + i) * LD(m.v + i);
+    if (determ <= 0.0) {
+        raise_error(m.result, i, PHASE_FORCES);
+        return;
+    }
+    double hg[8][4];
+    {
+        double dvdx[8], dvdy[8], dvdz[8];
+        volume_derivs(dvdx, dvdy, dvdz, x, y, z);
+        hourgam_all(hg, x, y, z, dvdx, dvdy, dvdz, 1.0 / determ);
+    }
+    const double coefficient =
+        -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) / cube_root(determ);
+    double vel[8], f[8];
+    gather8(m.xd, nl, vel);
+    fb_force_axis(hg, vel, coefficient, f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) m.fhx[k * N + i] = f[k];
+    gather8(m.yd, nl, vel);
+    fb_force_axis(hg, vel, coefficient, f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) m.fhy[k * N + i] = f[k];
+    gather8(m.zd, nl, vel);
+    fb_force_axis(hg, vel, coefficient, f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) m.fhz[k * N + i] = f[k];
+}
+
+// One node per thread: gather in CSR order, stress then hourglass per corner
+// (combineVolumeForcesTaskFunc, lulesh.cc:838-862), then the node update.
+__global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
+    if (m.dtime) {
+        if (!m.dtime->active) return;
+        dt = m.dtime->deltatime;
+    }
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= m.numNode) return;
+    const size_t N = (size_t)m.numElem;
+    const int b = LD(m.nodeElemStart + n), e = LD(m.nodeElemStart + n + 1);
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int j = b; j < e; ++j) {
+        const int c = LD(m.nodeElemCornerList + j);
+        const size_t idx = (size_t)(c & 7) * N + (size_t)(c >> 3);
+        fx += LD(m.fsx + idx);
+        fx += LD(m.fhx + idx);
+        fy += LD(m.fsy + idx);
+        fy += LD(m.fhy + idx);
+        fz += LD(m.fsz + idx);
+        fz += LD(m.fhz + idx);
+    }
+    node_update(m, n, fx, fy, fz, dt);
+}
+
+// CalcKinematicsForElemsTask (lulesh.cc:1169-1275) and
+// CalcMonotonicQGradientsForElemsTask (lulesh.cc:1277-1418) fused: both read
+// the same updated node positions and velocities.
+__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
+    if (m.dtime) {
+        if (!m.dtime->active) return;
+        dt = m.dtime->deltatime;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.numElem) return;
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    double x[8], y[8], z[8], xv[8], yv[8], zv[8];
+    gather8(m.x, nl, x);
+    gather8(m.y, nl, y);
+    gather8(m.z, nl, z);
+    const double volume = hex_volume(x, y, z);
+    const double relv = volume / LD(m.volo + i);
+    const double vold = m.v[i];
+    m.vnew[i] = relv;
+    m.delv[i] = relv - vold;
+    m.arealg[i] = 4.0 * volume / sqrt(max_face_area(x, y, z));
+
+    gather8(m.xd, nl, xv);
+    gather8(m.yd, nl, yv);
+    gather8(m.zd, nl, zv);
+    {
+        double g[6];
+        q_gradients(x, y, z, xv, yv, zv, LD(m.volo + i) * relv, g);
+        m.dvxi[i] = g[0];
+        m.dveta[i] = g[1];
+        m.dvzeta[i] = g[2];
+        m.dxxi[i] = g[3];
+        m.dxeta[i] = g[4];
+        m.dxzeta[i] = g[5];
+    }
+    const double dt2 = 0.5 * dt;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        x[k] -= dt2 * xv[k];
+        y[k] -= dt2 * yv[k];
+        z[k] -= dt2 * zv[k];
+    }
+    m.vdov[i] = vel_grad_trace(x, y, z, xv, yv, zv);
+    update_volume(m, i, vold, relv);
+}
+
+// Q limiter, EOS x rep, sound speed, save and dt minima; elements visited in
+// repeat-count order so a warp's lanes run the same number of EOS passes.
+__global__ void __launch_bounds__(kMatBlock) k_material(Mesh m) {
+    if (m.dtime && !m.dtime->active) return;
+    double dtc = 1.0e+20, dth = 1.0e+20;  // lulesh.cc:2214-2215
+    const int N = m.numElem;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+        const int i = LD(m.matOrder + t);
+        const double vnew = LD(m.vnew + i), vdov = LD(m.vdov + i);
+        double ql, qq;
+        q_terms<double>(m, i, m.dvxi, m.dveta, m.dvzeta, m.dxxi, m.dxeta, m.dxzeta, vnew, vdov, ql, qq);
+        m.qq[i] = qq;
+        m.ql[i] = ql;
+        double vnewc = vnew;
+        if (m.prm.eosvmin != 0.0 && vnewc < m.prm.eosvmin) vnewc = m.prm.eosvmin;
+        if (m.prm.eosvmax != 0.0 && vnewc > m.prm.eosvmax) vnewc = m.prm.eosvmax;
+        const double ss = eos_element(m, i, vnewc, LD(m.elemRep + i));
+        dt_constraints(m.prm, ss, vdov, LD(m.arealg + i), dtc, dth);
+    }
+    finish_dt_reduction(m, dtc, dth);
+}
+
+#undef LD
+
+int launch_forces(const Mesh& m, cudaStream_t s) {
+    k_forces<<<blocks_for(m.numElem, kForceBlock), kForceBlock, 0, s>>>(m);
+    return 1;
+}
+int launch_nodes(const Mesh& m, double dt, cudaStream_t s) {
+    k_nodes<<<blocks_for(m.numNode, kNodeBlock), kNodeBlock, 0, s>>>(m, dt);
+    return 1;
+}
+int launch_kinematics(const Mesh& m, double dt, cudaStream_t s) {
+    k_kinematics<<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt);
+    return 1;
+}
+int launch_material(const Mesh& m, cudaStream_t s) {
+    k_material<<<m.matGrid, kMatBlock, 0, s>>>(m);
+    return 1;
+}
+
+}  // namespace LULESH_VARIANT
+}  // namespace lulesh

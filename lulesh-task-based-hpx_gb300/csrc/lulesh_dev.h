@@ -1,0 +1,128 @@
+// Internal declarations shared by the device translation units.
+//
+// HBM layout (one handle, numElem = N_e, numNode = N_n):
+//   node SoA      x y z xd yd zd xdd ydd zdd fx fy fz nodalMass : double[N_n]
+//                 nodeSymm : uint8[N_n] (bit 0/1/2 = in symmX/Y/Z)
+//   element SoA   e p q ql qq v vnew delv vdov arealg ss volo elemMass : double[N_e]
+//                 nodelist : int32[8 N_e] (element-major, as Domain)
+//                 lxim..lzetap, elemBC : int32[N_e]
+//   CSR           nodeElemStart : int32[N_n+1], nodeElemCornerList : int32[8 N_e]
+//   material      matOrder : int32[N_e]  elements grouped by EOS repeat count
+//                 (largest first, ascending index within a group), elemRep : int32[N_e]
+//   scratch       corner forces, corner-major (index corner*N_e + elem):
+//                   double path: stress fsx fsy fsz and hourglass fhx fhy fhz
+//                   mixed path : combined float fcx fcy fcz
+//                 mixed path: float2 (hi, lo) mirrors of x y z xd yd zd[N_n]
+//                 gradients delv_xi.. delx_zeta: double[N_e] (float[N_e] mixed)
+//                 dt partial minima: one DtPartial per material block,
+//                 StepResult + block counter.
+// Corner-major corner forces make both the force kernel's stores and the
+// node gather's loads unit-stride across a warp on the structured mesh.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lulesh_gb300.h"
+
+namespace lulesh {
+
+// Boundary-condition bits of an element face (reference lulesh.h:46-74).
+constexpr int XI_M = 0x00007, XI_M_SYMM = 0x00001, XI_M_FREE = 0x00002, XI_M_COMM = 0x00004;
+constexpr int XI_P = 0x00038, XI_P_SYMM = 0x00008, XI_P_FREE = 0x00010, XI_P_COMM = 0x00020;
+constexpr int ETA_M = 0x001c0, ETA_M_SYMM = 0x00040, ETA_M_FREE = 0x00080, ETA_M_COMM = 0x00100;
+constexpr int ETA_P = 0x00e00, ETA_P_SYMM = 0x00200, ETA_P_FREE = 0x00400, ETA_P_COMM = 0x00800;
+constexpr int ZETA_M = 0x07000, ZETA_M_SYMM = 0x01000, ZETA_M_FREE = 0x02000, ZETA_M_COMM = 0x04000;
+constexpr int ZETA_P = 0x38000, ZETA_P_SYMM = 0x08000, ZETA_P_FREE = 0x10000, ZETA_P_COMM = 0x20000;
+
+// Phase ids recorded with a device error.
+constexpr int PHASE_FORCES = 1, PHASE_KINEMATICS = 2;
+
+struct DtPartial {
+    double dtc, dth;
+};
+
+// Written by the last material block; read by the host once per cycle.
+struct StepResult {
+    double dtcourant, dthydro;
+    int32_t err;       // 0 or LULESH_EVOLUME (first error wins)
+    int32_t err_elem;  // element that raised it
+    int32_t err_phase; // PHASE_*
+    uint32_t blocks_done;
+};
+
+// Device time state for the graph form (mirror of lulesh_time_state plus the
+// loop limit and a done flag).
+struct DevTime {
+    double time, deltatime, dtcourant, dthydro, dtfixed;
+    double deltatimemultlb, deltatimemultub, dtmax, stoptime;
+    int32_t cycle, max_cycles;
+    int32_t active;      // 1 while time < stoptime && cycle < max_cycles
+    int32_t pad_;
+};
+
+// Device pointers and sizes handed to every kernel by value.
+struct Mesh {
+    int32_t numElem, numNode;
+    // node-centred
+    double *x, *y, *z, *xd, *yd, *zd, *xdd, *ydd, *zdd, *fx, *fy, *fz;
+    const double* nodalMass;
+    const uint8_t* nodeSymm;
+    // element-centred
+    const int32_t* nodelist;
+    const int32_t *lxim, *lxip, *letam, *letap, *lzetam, *lzetap, *elemBC;
+    double *e, *p, *q, *ql, *qq, *v, *vnew, *delv, *vdov, *arealg, *ss;
+    const double *volo, *elemMass;
+    const int32_t *nodeElemStart, *nodeElemCornerList;
+    const int32_t *matOrder, *elemRep;
+    // scratch, double path
+    double *fsx, *fsy, *fsz, *fhx, *fhy, *fhz;
+    double *dvxi, *dveta, *dvzeta, *dxxi, *dxeta, *dxzeta;
+    // mixed path: float-pair mirrors (hi, lo) of positions and velocities
+    float2 *pxp, *pyp, *pzp, *vxp, *vyp, *vzp;
+    // scratch, mixed path
+    float *fcx, *fcy, *fcz;
+    float *gvxi, *gveta, *gvzeta, *gxxi, *gxeta, *gxzeta;
+    // reduction scratch
+    DtPartial* partials;
+    StepResult* result;
+    DevTime* dtime;  // non-null only in the graph form: kernels take dt from here
+    int32_t matGrid; // blocks of the material kernel (= entries of partials)
+    lulesh_params prm;
+};
+
+// Launch configuration shared by host and device code.
+constexpr int kForceBlock = 128;
+constexpr int kNodeBlock = 256;
+constexpr int kKinBlock = 128;
+constexpr int kMatBlock = 128;
+
+inline int blocks_for(int n, int b) { return (n + b - 1) / b; }
+
+// Launchers, one set per arithmetic variant. Each returns the number of
+// kernels it launched. `dt` is used unless m.dtime is set.
+namespace fp64 {
+int launch_forces(const Mesh& m, cudaStream_t s);
+int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
+int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
+int launch_material(const Mesh& m, cudaStream_t s);
+}  // namespace fp64
+namespace fp64x {
+int launch_forces(const Mesh& m, cudaStream_t s);
+int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
+int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
+int launch_material(const Mesh& m, cudaStream_t s);
+}  // namespace fp64x
+namespace mixed {
+int launch_forces(const Mesh& m, cudaStream_t s);
+int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
+int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
+int launch_material(const Mesh& m, cudaStream_t s);
+int launch_mirror(const Mesh& m, cudaStream_t s);
+}  // namespace mixed
+
+// Device-side TimeIncrement for the graph form (time_increment.cu).
+int launch_time_increment(DevTime* t, StepResult* r, cudaStream_t s);
+int launch_time_finish(DevTime* t, StepResult* r, cudaStream_t s);
+
+}  // namespace lulesh

@@ -1,0 +1,637 @@
+// Element, node and material arithmetic shared by the step kernels.
+//
+// Every function lives in namespace lulesh::LULESH_VARIANT, so the three
+// translation units that include this header (fast double, exact double
+// compiled with --fmad=false, mixed) never share an out-of-line copy compiled
+// with another contraction setting.
+//
+// Geometry functions are templated on the real type R (double for the double
+// paths, float for the mixed path's temporaries) and keep the reference's
+// operand order and parenthesisation (esa-tu-darmstadt/lulesh-task-based-hpx
+// lulesh.cc), which is what makes the exact double variant round every
+// operation as the reference does.
+#pragma once
+
+#include "lulesh_dev.h"
+#include "portable_cbrt.h"
+
+#ifndef LULESH_VARIANT
+#error "define LULESH_VARIANT"
+#endif
+
+namespace lulesh {
+namespace LULESH_VARIANT {
+
+#define LD(p) __ldg(p)
+
+__device__ __forceinline__ void raise_error(StepResult* r, int elem, int phase) {
+    if (atomicCAS(&r->err, 0, LULESH_EVOLUME) == 0) {
+        r->err_elem = elem;
+        r->err_phase = phase;
+    }
+}
+
+__device__ __forceinline__ void load_nodelist(const int32_t* nodelist, int i, int nl[8]) {
+    const int4* p = reinterpret_cast<const int4*>(nodelist + 8 * (size_t)i);
+    const int4 a = __ldg(p), b = __ldg(p + 1);
+    nl[0] = a.x; nl[1] = a.y; nl[2] = a.z; nl[3] = a.w;
+    nl[4] = b.x; nl[5] = b.y; nl[6] = b.z; nl[7] = b.w;
+}
+
+__device__ __forceinline__ void gather8(const double* __restrict__ f, const int nl[8], double o[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o[k] = LD(f + nl[k]);
+}
+
+// --- element geometry -------------------------------------------------------
+
+// TRIPLE_PRODUCT of lulesh.cc:649-651, arguments in the macro's order.
+template <class R>
+__device__ __forceinline__ R triple(R x1, R y1, R z1, R x2, R y2, R z2, R x3, R y3, R z3) {
+    return x1 * (y2 * z3 - z2 * y3) + x2 * (z1 * y3 - y1 * z3) + x3 * (y1 * z2 - z1 * y2);
+}
+
+// CalcElemVolume (lulesh.cc:592-665).
+template <class R>
+__device__ __forceinline__ R hex_volume(const R x[8], const R y[8], const R z[8]) {
+    const R twelveth = R(1.0) / R(12.0);
+    R dx61 = x[6] - x[1], dy61 = y[6] - y[1], dz61 = z[6] - z[1];
+    R dx70 = x[7] - x[0], dy70 = y[7] - y[0], dz70 = z[7] - z[0];
+    R dx63 = x[6] - x[3], dy63 = y[6] - y[3], dz63 = z[6] - z[3];
+    R dx20 = x[2] - x[0], dy20 = y[2] - y[0], dz20 = z[2] - z[0];
+    R dx50 = x[5] - x[0], dy50 = y[5] - y[0], dz50 = z[5] - z[0];
+    R dx64 = x[6] - x[4], dy64 = y[6] - y[4], dz64 = z[6] - z[4];
+    R dx31 = x[3] - x[1], dy31 = y[3] - y[1], dz31 = z[3] - z[1];
+    R dx72 = x[7] - x[2], dy72 = y[7] - y[2], dz72 = z[7] - z[2];
+    R dx43 = x[4] - x[3], dy43 = y[4] - y[3], dz43 = z[4] - z[3];
+    R dx57 = x[5] - x[7], dy57 = y[5] - y[7], dz57 = z[5] - z[7];
+    R dx14 = x[1] - x[4], dy14 = y[1] - y[4], dz14 = z[1] - z[4];
+    R dx25 = x[2] - x[5], dy25 = y[2] - y[5], dz25 = z[2] - z[5];
+    R vol = triple(dx31 + dx72, dx63, dx20, dy31 + dy72, dy63, dy20, dz31 + dz72, dz63, dz20) +
+            triple(dx43 + dx57, dx64, dx70, dy43 + dy57, dy64, dy70, dz43 + dz57, dz64, dz70) +
+            triple(dx14 + dx25, dx61, dx50, dy14 + dy25, dy61, dy50, dz14 + dz25, dz61, dz50);
+    vol *= twelveth;
+    return vol;
+}
+
+// Centre Jacobian of CalcElemShapeFunctionDerivatives (lulesh.cc:277-305).
+template <class R>
+struct Jac {
+    R fjxxi, fjxet, fjxze, fjyxi, fjyet, fjyze, fjzxi, fjzet, fjzze;
+};
+
+template <class R>
+__device__ __forceinline__ Jac<R> jacobian(const R x[8], const R y[8], const R z[8]) {
+    const R c = R(.125);
+    Jac<R> j;
+    j.fjxxi = c * ((x[6] - x[0]) + (x[5] - x[3]) - (x[7] - x[1]) - (x[4] - x[2]));
+    j.fjxet = c * ((x[6] - x[0]) - (x[5] - x[3]) + (x[7] - x[1]) - (x[4] - x[2]));
+    j.fjxze = c * ((x[6] - x[0]) + (x[5] - x[3]) + (x[7] - x[1]) + (x[4] - x[2]));
+    j.fjyxi = c * ((y[6] - y[0]) + (y[5] - y[3]) - (y[7] - y[1]) - (y[4] - y[2]));
+    j.fjyet = c * ((y[6] - y[0]) - (y[5] - y[3]) + (y[7] - y[1]) - (y[4] - y[2]));
+    j.fjyze = c * ((y[6] - y[0]) + (y[5] - y[3]) + (y[7] - y[1]) + (y[4] - y[2]));
+    j.fjzxi = c * ((z[6] - z[0]) + (z[5] - z[3]) - (z[7] - z[1]) - (z[4] - z[2]));
+    j.fjzet = c * ((z[6] - z[0]) - (z[5] - z[3]) + (z[7] - z[1]) - (z[4] - z[2]));
+    j.fjzze = c * ((z[6] - z[0]) + (z[5] - z[3]) + (z[7] - z[1]) + (z[4] - z[2]));
+    return j;
+}
+
+// Determinant only (lulesh.cc:308-373 without the B matrix).
+template <class R>
+__device__ __forceinline__ R jac_det(const Jac<R>& j) {
+    const R cjxet = -(j.fjyxi * j.fjzze) + (j.fjzxi * j.fjyze);
+    const R cjyet = (j.fjxxi * j.fjzze) - (j.fjzxi * j.fjxze);
+    const R cjzet = -(j.fjxxi * j.fjyze) + (j.fjyxi * j.fjxze);
+    return R(8.) * (j.fjxet * cjxet + j.fjyet * cjyet + j.fjzet * cjzet);
+}
+
+// Shape-function derivatives b[a][0..3] (b[a][4..7] are their negatives,
+// lulesh.cc:337-364) and the determinant.
+template <class R>
+__device__ __forceinline__ R shape_derivs(const Jac<R>& j, R b[3][4]) {
+    const R cjxxi = (j.fjyet * j.fjzze) - (j.fjzet * j.fjyze);
+    const R cjxet = -(j.fjyxi * j.fjzze) + (j.fjzxi * j.fjyze);
+    const R cjxze = (j.fjyxi * j.fjzet) - (j.fjzxi * j.fjyet);
+    const R cjyxi = -(j.fjxet * j.fjzze) + (j.fjzet * j.fjxze);
+    const R cjyet = (j.fjxxi * j.fjzze) - (j.fjzxi * j.fjxze);
+    const R cjyze = -(j.fjxxi * j.fjzet) + (j.fjzxi * j.fjxet);
+    const R cjzxi = (j.fjxet * j.fjyze) - (j.fjyet * j.fjxze);
+    const R cjzet = -(j.fjxxi * j.fjyze) + (j.fjyxi * j.fjxze);
+    const R cjzze = (j.fjxxi * j.fjyet) - (j.fjyxi * j.fjxet);
+    b[0][0] = -cjxxi - cjxet - cjxze;
+    b[0][1] = cjxxi - cjxet - cjxze;
+    b[0][2] = cjxxi + cjxet - cjxze;
+    b[0][3] = -cjxxi + cjxet - cjxze;
+    b[1][0] = -cjyxi - cjyet - cjyze;
+    b[1][1] = cjyxi - cjyet - cjyze;
+    b[1][2] = cjyxi + cjyet - cjyze;
+    b[1][3] = -cjyxi + cjyet - cjyze;
+    b[2][0] = -cjzxi - cjzet - cjzze;
+    b[2][1] = cjzxi - cjzet - cjzze;
+    b[2][2] = cjzxi + cjzet - cjzze;
+    b[2][3] = -cjzxi + cjzet - cjzze;
+    return R(8.) * (j.fjxet * cjxet + j.fjyet * cjyet + j.fjzet * cjzet);
+}
+
+// One face's area vector added to its four corners (SumElemFaceNormal,
+// lulesh.cc:378-409); A..D are the face corners in the reference's order.
+template <int A, int B, int C, int D, class R>
+__device__ __forceinline__ void face_normal(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
+                                            const R z[8]) {
+    const R bisX0 = R(0.5) * (x[D] + x[C] - x[B] - x[A]);
+    const R bisY0 = R(0.5) * (y[D] + y[C] - y[B] - y[A]);
+    const R bisZ0 = R(0.5) * (z[D] + z[C] - z[B] - z[A]);
+    const R bisX1 = R(0.5) * (x[C] + x[B] - x[D] - x[A]);
+    const R bisY1 = R(0.5) * (y[C] + y[B] - y[D] - y[A]);
+    const R bisZ1 = R(0.5) * (z[C] + z[B] - z[D] - z[A]);
+    const R ax = R(0.25) * (bisY0 * bisZ1 - bisZ0 * bisY1);
+    const R ay = R(0.25) * (bisZ0 * bisX1 - bisX0 * bisZ1);
+    const R az = R(0.25) * (bisX0 * bisY1 - bisY0 * bisX1);
+    nx[A] += ax; nx[B] += ax; nx[C] += ax; nx[D] += ax;
+    ny[A] += ay; ny[B] += ay; ny[C] += ay; ny[D] += ay;
+    nz[A] += az; nz[B] += az; nz[C] += az; nz[D] += az;
+}
+
+// CalcElemNodeNormals (lulesh.cc:413-451), faces in the reference's order.
+template <class R>
+__device__ __forceinline__ void node_normals(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
+                                             const R z[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) nx[k] = ny[k] = nz[k] = R(0.0);
+    face_normal<0, 1, 2, 3>(nx, ny, nz, x, y, z);
+    face_normal<0, 4, 5, 1>(nx, ny, nz, x, y, z);
+    face_normal<1, 5, 6, 2>(nx, ny, nz, x, y, z);
+    face_normal<2, 6, 7, 3>(nx, ny, nz, x, y, z);
+    face_normal<3, 7, 4, 0>(nx, ny, nz, x, y, z);
+    face_normal<4, 7, 6, 5>(nx, ny, nz, x, y, z);
+}
+
+// VoluDer (lulesh.cc:468-491) for corner K from the corners P0..P5.
+template <int K, int P0, int P1, int P2, int P3, int P4, int P5, class R>
+__device__ __forceinline__ void volu_der(R dvdx[8], R dvdy[8], R dvdz[8], const R x[8],
+                                         const R y[8], const R z[8]) {
+    const R twelfth = R(1.0) / R(12.0);
+    const R x0 = x[P0], x1 = x[P1], x2 = x[P2], x3 = x[P3], x4 = x[P4], x5 = x[P5];
+    const R y0 = y[P0], y1 = y[P1], y2 = y[P2], y3 = y[P3], y4 = y[P4], y5 = y[P5];
+    const R z0 = z[P0], z1 = z[P1], z2 = z[P2], z3 = z[P3], z4 = z[P4], z5 = z[P5];
+    const R dx = (y1 + y2) * (z0 + z1) - (y0 + y1) * (z1 + z2) + (y0 + y4) * (z3 + z4) -
+                 (y3 + y4) * (z0 + z4) - (y2 + y5) * (z3 + z5) + (y3 + y5) * (z2 + z5);
+    const R dy = -(x1 + x2) * (z0 + z1) + (x0 + x1) * (z1 + z2) - (x0 + x4) * (z3 + z4) +
+                 (x3 + x4) * (z0 + z4) + (x2 + x5) * (z3 + z5) - (x3 + x5) * (z2 + z5);
+    const R dz = -(y1 + y2) * (x0 + x1) + (y0 + y1) * (x1 + x2) - (y0 + y4) * (x3 + x4) +
+                 (y3 + y4) * (x0 + x4) + (y2 + y5) * (x3 + x5) - (y3 + y5) * (x2 + x5);
+    dvdx[K] = dx * twelfth;
+    dvdy[K] = dy * twelfth;
+    dvdz[K] = dz * twelfth;
+}
+
+// CalcElemVolumeDerivative (lulesh.cc:495-523).
+template <class R>
+__device__ __forceinline__ void volume_derivs(R dvdx[8], R dvdy[8], R dvdz[8], const R x[8],
+                                              const R y[8], const R z[8]) {
+    volu_der<0, 1, 2, 3, 4, 5, 7>(dvdx, dvdy, dvdz, x, y, z);
+    volu_der<3, 0, 1, 2, 7, 4, 6>(dvdx, dvdy, dvdz, x, y, z);
+    volu_der<2, 3, 0, 1, 6, 7, 5>(dvdx, dvdy, dvdz, x, y, z);
+    volu_der<1, 2, 3, 0, 5, 6, 4>(dvdx, dvdy, dvdz, x, y, z);
+    volu_der<4, 7, 6, 5, 0, 3, 1>(dvdx, dvdy, dvdz, x, y, z);
+    volu_der<5, 4, 7, 6, 1, 0, 2>(dvdx, dvdy, dvdz, x, y, z);
+    volu_der<6, 5, 4, 7, 2, 1, 3>(dvdx, dvdy, dvdz, x, y, z);
+    volu_der<7, 6, 5, 4, 3, 2, 0>(dvdx, dvdy, dvdz, x, y, z);
+}
+
+// Flanagan-Belytschko hourglass base vector M at corner k (lulesh.cc:921-954):
+//   {1,1,-1,-1,-1,-1,1,1} {1,-1,-1,1,-1,1,1,-1} {1,-1,1,-1,1,-1,1,-1} {-1,1,-1,1,1,-1,1,-1}
+__host__ __device__ constexpr int gamma_sign(int M, int k) {
+    return (M == 0)   ? ((k == 2 || k == 3 || k == 4 || k == 5) ? -1 : 1)
+           : (M == 1) ? ((k == 1 || k == 2 || k == 4 || k == 7) ? -1 : 1)
+           : (M == 2) ? ((k & 1) ? -1 : 1)
+                      : ((k == 0 || k == 2 || k == 5 || k == 7) ? -1 : 1);
+}
+
+// Sum_k v[k] * gamma[M][k] in the reference's left-to-right order
+// (lulesh.cc:972-986); the products by +-1 are exact.
+template <int M, class R>
+__device__ __forceinline__ R hourmod(const R v[8]) {
+    return v[0] * R(gamma_sign(M, 0)) + v[1] * R(gamma_sign(M, 1)) + v[2] * R(gamma_sign(M, 2)) +
+           v[3] * R(gamma_sign(M, 3)) + v[4] * R(gamma_sign(M, 4)) + v[5] * R(gamma_sign(M, 5)) +
+           v[6] * R(gamma_sign(M, 6)) + v[7] * R(gamma_sign(M, 7));
+}
+
+// Hourglass shape vectors of mode M (lulesh.cc:988-1023).
+template <int M, class R>
+__device__ __forceinline__ void hourgam_mode(R hg[8][4], const R x[8], const R y[8], const R z[8],
+                                             const R dvdx[8], const R dvdy[8], const R dvdz[8],
+                                             R volinv) {
+    const R hx = hourmod<M>(x), hy = hourmod<M>(y), hz = hourmod<M>(z);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        hg[k][M] = R(gamma_sign(M, k)) - volinv * (dvdx[k] * hx + dvdy[k] * hy + dvdz[k] * hz);
+}
+
+template <class R>
+__device__ __forceinline__ void hourgam_all(R hg[8][4], const R x[8], const R y[8], const R z[8],
+                                            const R dvdx[8], const R dvdy[8], const R dvdz[8],
+                                            R volinv) {
+    hourgam_mode<0>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
+    hourgam_mode<1>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
+    hourgam_mode<2>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
+    hourgam_mode<3>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
+}
+
+// CalcElemFBHourglassForce for one axis (lulesh.cc:527-562).
+template <class R>
+__device__ __forceinline__ void fb_force_axis(const R hg[8][4], const R vel[8], R coefficient,
+                                              R out[8]) {
+    R h[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+        h[m] = hg[0][m] * vel[0] + hg[1][m] * vel[1] + hg[2][m] * vel[2] + hg[3][m] * vel[3] +
+               hg[4][m] * vel[4] + hg[5][m] * vel[5] + hg[6][m] * vel[6] + hg[7][m] * vel[7];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        out[k] = coefficient * (hg[k][0] * h[0] + hg[k][1] * h[1] + hg[k][2] * h[2] + hg[k][3] * h[3]);
+}
+
+// AreaFace (lulesh.cc:678-692) of the face with corners A..D.
+template <int A, int B, int C, int D, class R>
+__device__ __forceinline__ R face_area(const R x[8], const R y[8], const R z[8]) {
+    const R fx = (x[C] - x[A]) - (x[D] - x[B]);
+    const R fy = (y[C] - y[A]) - (y[D] - y[B]);
+    const R fz = (z[C] - z[A]) - (z[D] - z[B]);
+    const R gx = (x[C] - x[A]) + (x[D] - x[B]);
+    const R gy = (y[C] - y[A]) + (y[D] - y[B]);
+    const R gz = (z[C] - z[A]) + (z[D] - z[B]);
+    return (fx * fx + fy * fy + fz * fz) * (gx * gx + gy * gy + gz * gz) -
+           (fx * gx + fy * gy + fz * gz) * (fx * gx + fy * gy + fz * gz);
+}
+
+template <class R>
+__device__ __forceinline__ R max_ref(R a, R cl) {
+    return (a < cl) ? cl : a;  // std::max(a, cl)
+}
+
+// Largest face measure of CalcElemCharacteristicLength (lulesh.cc:696-729);
+// the characteristic length is 4 V / sqrt(of it).
+template <class R>
+__device__ __forceinline__ R max_face_area(const R x[8], const R y[8], const R z[8]) {
+    R cl = R(0.0);
+    cl = max_ref(face_area<0, 1, 2, 3>(x, y, z), cl);
+    cl = max_ref(face_area<4, 5, 6, 7>(x, y, z), cl);
+    cl = max_ref(face_area<0, 1, 5, 4>(x, y, z), cl);
+    cl = max_ref(face_area<1, 2, 6, 5>(x, y, z), cl);
+    cl = max_ref(face_area<2, 3, 7, 6>(x, y, z), cl);
+    cl = max_ref(face_area<3, 0, 4, 7>(x, y, z), cl);
+    return cl;
+}
+
+// Monotonic-Q gradients of CalcMonotonicQGradientsForElemsTask
+// (lulesh.cc:1341-1416). vol = volo * vnew. Outputs
+// g[0..2] = delv_xi, delv_eta, delv_zeta and g[3..5] = delx_xi, delx_eta, delx_zeta.
+template <class R>
+__device__ __forceinline__ void q_gradients(const R x[8], const R y[8], const R z[8], const R xv[8],
+                                            const R yv[8], const R zv[8], R vol, R g[6]) {
+    const R ptiny = R(1.e-36);
+    const R q = R(0.25), mq = R(-0.25);
+    const R norm = R(1.0) / (vol + ptiny);
+    const R dxj = mq * ((x[0] + x[1] + x[5] + x[4]) - (x[3] + x[2] + x[6] + x[7]));
+    const R dyj = mq * ((y[0] + y[1] + y[5] + y[4]) - (y[3] + y[2] + y[6] + y[7]));
+    const R dzj = mq * ((z[0] + z[1] + z[5] + z[4]) - (z[3] + z[2] + z[6] + z[7]));
+    const R dxi = q * ((x[1] + x[2] + x[6] + x[5]) - (x[0] + x[3] + x[7] + x[4]));
+    const R dyi = q * ((y[1] + y[2] + y[6] + y[5]) - (y[0] + y[3] + y[7] + y[4]));
+    const R dzi = q * ((z[1] + z[2] + z[6] + z[5]) - (z[0] + z[3] + z[7] + z[4]));
+    const R dxk = q * ((x[4] + x[5] + x[6] + x[7]) - (x[0] + x[1] + x[2] + x[3]));
+    const R dyk = q * ((y[4] + y[5] + y[6] + y[7]) - (y[0] + y[1] + y[2] + y[3]));
+    const R dzk = q * ((z[4] + z[5] + z[6] + z[7]) - (z[0] + z[1] + z[2] + z[3]));
+    R ax, ay, az, dxv, dyv, dzv;
+
+    // zeta: i cross j
+    ax = dyi * dzj - dzi * dyj;
+    ay = dzi * dxj - dxi * dzj;
+    az = dxi * dyj - dyi * dxj;
+    g[5] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
+    ax *= norm;
+    ay *= norm;
+    az *= norm;
+    dxv = q * ((xv[4] + xv[5] + xv[6] + xv[7]) - (xv[0] + xv[1] + xv[2] + xv[3]));
+    dyv = q * ((yv[4] + yv[5] + yv[6] + yv[7]) - (yv[0] + yv[1] + yv[2] + yv[3]));
+    dzv = q * ((zv[4] + zv[5] + zv[6] + zv[7]) - (zv[0] + zv[1] + zv[2] + zv[3]));
+    g[2] = ax * dxv + ay * dyv + az * dzv;
+
+    // xi: j cross k
+    ax = dyj * dzk - dzj * dyk;
+    ay = dzj * dxk - dxj * dzk;
+    az = dxj * dyk - dyj * dxk;
+    g[3] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
+    ax *= norm;
+    ay *= norm;
+    az *= norm;
+    dxv = q * ((xv[1] + xv[2] + xv[6] + xv[5]) - (xv[0] + xv[3] + xv[7] + xv[4]));
+    dyv = q * ((yv[1] + yv[2] + yv[6] + yv[5]) - (yv[0] + yv[3] + yv[7] + yv[4]));
+    dzv = q * ((zv[1] + zv[2] + zv[6] + zv[5]) - (zv[0] + zv[3] + zv[7] + zv[4]));
+    g[0] = ax * dxv + ay * dyv + az * dzv;
+
+    // eta: k cross i
+    ax = dyk * dzi - dzk * dyi;
+    ay = dzk * dxi - dxk * dzi;
+    az = dxk * dyi - dyk * dxi;
+    g[4] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
+    ax *= norm;
+    ay *= norm;
+    az *= norm;
+    dxv = mq * ((xv[0] + xv[1] + xv[5] + xv[4]) - (xv[3] + xv[2] + xv[6] + xv[7]));
+    dyv = mq * ((yv[0] + yv[1] + yv[5] + yv[4]) - (yv[3] + yv[2] + yv[6] + yv[7]));
+    dzv = mq * ((zv[0] + zv[1] + zv[5] + zv[4]) - (zv[3] + zv[2] + zv[6] + zv[7]));
+    g[1] = ax * dxv + ay * dyv + az * dzv;
+}
+
+// Trace of the velocity gradient at the half-step geometry
+// (CalcElemVelocityGradient lulesh.cc:733-781, d[0]+d[1]+d[2] as
+// lulesh.cc:1232). xh.. are the half-step coordinates.
+template <class R>
+__device__ __forceinline__ R vel_grad_trace(const R xh[8], const R yh[8], const R zh[8],
+                                            const R xv[8], const R yv[8], const R zv[8]) {
+    R b[3][4];
+    const R detJ = shape_derivs(jacobian(xh, yh, zh), b);
+    const R inv = R(1.0) / detJ;
+    const R dxx = inv * (b[0][0] * (xv[0] - xv[6]) + b[0][1] * (xv[1] - xv[7]) +
+                         b[0][2] * (xv[2] - xv[4]) + b[0][3] * (xv[3] - xv[5]));
+    const R dyy = inv * (b[1][0] * (yv[0] - yv[6]) + b[1][1] * (yv[1] - yv[7]) +
+                         b[1][2] * (yv[2] - yv[4]) + b[1][3] * (yv[3] - yv[5]));
+    const R dzz = inv * (b[2][0] * (zv[0] - zv[6]) + b[2][1] * (zv[1] - zv[7]) +
+                         b[2][2] * (zv[2] - zv[4]) + b[2][3] * (zv[3] - zv[5]));
+    return dxx + dyy + dzz;
+}
+
+// --- material ------------------------------------------------------------
+
+// Monotonic limiter of one direction (lulesh.cc:1464-1531, repeated for eta
+// and zeta): dv is the direction's velocity gradient, bm/bp the minus/plus
+// face BC bits, nm/np the face neighbours.
+template <class R>
+__device__ __forceinline__ R limiter(const R* __restrict__ dv, int i, int bm, int bp, int symm_m,
+                                     int comm_m, int nm, int symm_p, int comm_p, int np, R mult,
+                                     R max_slope) {
+    const R ptiny = R(1.e-36);
+    const R self = LD(dv + i);
+    const R norm = R(1.) / (self + ptiny);
+    R delvm, delvp;
+    if (bm == comm_m || bm == 0) delvm = LD(dv + nm);
+    else if (bm == symm_m) delvm = self;
+    else delvm = R(0.0);  // free surface (and malformed masks, lulesh.cc:1477-1480)
+    if (bp == comm_p || bp == 0) delvp = LD(dv + np);
+    else if (bp == symm_p) delvp = self;
+    else delvp = R(0.0);
+    delvm = delvm * norm;
+    delvp = delvp * norm;
+    R phi = R(.5) * (delvm + delvp);
+    delvm *= mult;
+    delvp *= mult;
+    if (delvm < phi) phi = delvm;
+    if (delvp < phi) phi = delvp;
+    if (phi < R(0.)) phi = R(0.);
+    if (phi > max_slope) phi = max_slope;
+    return phi;
+}
+
+// Linear and quadratic q of one element (lulesh.cc:1448-1656). dv/dx are the
+// six gradient arrays.
+template <class R>
+__device__ __forceinline__ void q_terms(const Mesh& m, int i, const R* dvxi, const R* dveta,
+                                        const R* dvzeta, const R* dxxi, const R* dxeta,
+                                        const R* dxzeta, double vnew, double vdov, double& ql,
+                                        double& qq) {
+    const lulesh_params& P = m.prm;
+    const int bc = LD(m.elemBC + i);
+    const R mult = R(P.monoq_limiter_mult), slope = R(P.monoq_max_slope);
+    const R phixi = limiter(dvxi, i, bc & XI_M, bc & XI_P, XI_M_SYMM, XI_M_COMM, LD(m.lxim + i),
+                            XI_P_SYMM, XI_P_COMM, LD(m.lxip + i), mult, slope);
+    const R phieta = limiter(dveta, i, bc & ETA_M, bc & ETA_P, ETA_M_SYMM, ETA_M_COMM,
+                             LD(m.letam + i), ETA_P_SYMM, ETA_P_COMM, LD(m.letap + i), mult, slope);
+    const R phizeta = limiter(dvzeta, i, bc & ZETA_M, bc & ZETA_P, ZETA_M_SYMM, ZETA_M_COMM,
+                              LD(m.lzetam + i), ZETA_P_SYMM, ZETA_P_COMM, LD(m.lzetap + i), mult,
+                              slope);
+    if (vdov > 0.) {
+        ql = 0.;
+        qq = 0.;
+        return;
+    }
+    R dxi = LD(dvxi + i) * LD(dxxi + i);
+    R deta = LD(dveta + i) * LD(dxeta + i);
+    R dzeta = LD(dvzeta + i) * LD(dxzeta + i);
+    if (dxi > R(0.)) dxi = R(0.);
+    if (deta > R(0.)) deta = R(0.);
+    if (dzeta > R(0.)) dzeta = R(0.);
+    const R rho = R(LD(m.elemMass + i) / (LD(m.volo + i) * vnew));
+    const R qlin = -R(P.qlc_monoq) * rho *
+                   (dxi * (R(1.) - phixi) + deta * (R(1.) - phieta) + dzeta * (R(1.) - phizeta));
+    const R qquad = R(P.qqc_monoq) * rho *
+                    (dxi * dxi * (R(1.) - phixi * phixi) + deta * deta * (R(1.) - phieta * phieta) +
+                     dzeta * dzeta * (R(1.) - phizeta * phizeta));
+    ql = double(qlin);
+    qq = double(qquad);
+}
+
+// CalcPressureForElemsTask for one element (lulesh.cc:1671-1690).
+__device__ __forceinline__ double eos_pressure(double& bvc, double& pbvc, double e, double comp,
+                                               double vnewc, const lulesh_params& P) {
+    const double cls = 2.0 / 3.0;
+    bvc = cls * (comp + 1.0);
+    pbvc = cls;
+    double nv = bvc * e;
+    if (fabs(nv) < P.p_cut || vnewc >= P.eosvmax) nv = 0.0;
+    if (nv < P.pmin) nv = P.pmin;
+    return nv;
+}
+
+__device__ __forceinline__ double ss_guard(double ssc) {
+    return (ssc <= .1111111e-36) ? .3333333e-18 : sqrt(ssc);
+}
+
+// rep evaluations of EvalEOSAllInOneTask (lulesh.cc:1692-1871) for element i,
+// each from the saved state, then the sound speed and the save of
+// CalcSoundSpeedForElemsAndSaveTask (lulesh.cc:1873-1904). Returns ss.
+__device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc, int rep) {
+    const lulesh_params& P = m.prm;
+    double e_new = 0., p_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
+    for (int r = 0; r < rep; ++r) {
+        // Each evaluation re-reads its inputs from memory as the reference's
+        // EvalEOSInit does (lulesh.cc:1720-1727); the barrier keeps the
+        // compiler from hoisting the loop-invariant evaluation out of the
+        // repeat loop, so the repeat count stays real work.
+        asm volatile("" ::: "memory");
+        const double e_old = m.e[i], delvc = m.delv[i], q_old = m.q[i];
+        double p_old = m.p[i];
+        const double qq_old = m.qq[i], ql_old = m.ql[i];
+        double comp = 1. / vnewc - 1.;
+        const double vchalf = vnewc - delvc * .5;
+        double compHalf = 1. / vchalf - 1.;
+        if (P.eosvmin != 0. && vnewc <= P.eosvmin) compHalf = comp;
+        if (P.eosvmax != 0.0 && vnewc >= P.eosvmax) {
+            p_old = 0.;
+            comp = 0.;
+            compHalf = 0.;
+        }
+        // predictor; the reference's "+ 0.5 * work" term adds 0.5 * 0
+        e_new = e_old - 0.5 * delvc * (p_old + q_old) + 0.5 * 0.0;
+        if (e_new < P.emin) e_new = P.emin;
+        const double pHalf = eos_pressure(bvc, pbvc, e_new, compHalf, vnewc, P);
+        const double vhalf = 1. / (1. + compHalf);
+        if (delvc > 0.) {
+            q_new = 0.;
+        } else {
+            const double ssc = ss_guard((pbvc * e_new + vhalf * vhalf * bvc * pHalf) / P.refdens);
+            q_new = (ssc * ql_old + qq_old);
+        }
+        e_new = e_new + 0.5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (pHalf + q_new));
+        e_new = e_new + 0.5 * 0.0;
+        if (fabs(e_new) < P.e_cut) e_new = 0.0;
+        if (e_new < P.emin) e_new = P.emin;
+        p_new = eos_pressure(bvc, pbvc, e_new, comp, vnewc, P);
+        // corrector
+        {
+            const double sixth = 1.0 / 6.0;
+            double q_tilde;
+            if (delvc > 0.) {
+                q_tilde = 0.;
+            } else {
+                const double ssc = ss_guard((pbvc * e_new + vnewc * vnewc * bvc * p_new) / P.refdens);
+                q_tilde = (ssc * ql_old + qq_old);
+            }
+            e_new = e_new -
+                    (7.0 * (p_old + q_old) - 8.0 * (pHalf + q_new) + (p_new + q_tilde)) * delvc * sixth;
+            if (fabs(e_new) < P.e_cut) e_new = 0.;
+            if (e_new < P.emin) e_new = P.emin;
+        }
+        p_new = eos_pressure(bvc, pbvc, e_new, comp, vnewc, P);
+        if (delvc <= 0.) {
+            const double ssc = ss_guard((pbvc * e_new + vnewc * vnewc * bvc * p_new) / P.refdens);
+            q_new = (ssc * ql_old + qq_old);
+            if (fabs(q_new) < P.q_cut) q_new = 0.;
+        }
+    }
+    const double sst = ss_guard((pbvc * e_new + vnewc * vnewc * bvc * p_new) / P.refdens);
+    m.ss[i] = sst;
+    m.p[i] = p_new;
+    m.e[i] = e_new;
+    m.q[i] = q_new;
+    return sst;
+}
+
+// Courant and hydro constraints of one element (lulesh.cc:1938-1974),
+// folded into running minima; vdov == 0 elements do not constrain.
+__device__ __forceinline__ void dt_constraints(const lulesh_params& P, double ss, double vdov,
+                                               double arealg, double& dtc, double& dth) {
+    if (vdov == 0.0) return;
+    const double qqc2 = 64.0 * P.qqc * P.qqc;
+    double dtf = ss * ss;
+    if (vdov < 0.0) dtf += qqc2 * arealg * arealg * vdov * vdov;
+    dtf = sqrt(dtf);
+    dtf = arealg / dtf;
+    dtc = fmin(dtc, dtf);
+    dth = fmin(dth, P.dvovmax / (fabs(vdov) + 1.e-20));
+}
+
+// Block-wide min of (a, b); the result is valid in thread 0.
+__device__ __forceinline__ void block_min2(double& a, double& b) {
+    __shared__ double sa[32], sb[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmin(a, __shfl_down_sync(0xffffffffu, a, o));
+        b = fmin(b, __shfl_down_sync(0xffffffffu, b, o));
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sa[w] = a;
+        sb[w] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        a = lane < nw ? sa[lane] : 1.0e+20;
+        b = lane < nw ? sb[lane] : 1.0e+20;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a = fmin(a, __shfl_down_sync(0xffffffffu, a, o));
+            b = fmin(b, __shfl_down_sync(0xffffffffu, b, o));
+        }
+    }
+}
+
+// Publishes this block's (dtc, dth) minima; the last block to arrive reduces
+// all partials into m.result and re-arms the counter. One pass, no second
+// launch. Every thread of the block must call it.
+__device__ __forceinline__ void finish_dt_reduction(const Mesh& m, double dtc, double dth) {
+    block_min2(dtc, dth);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        m.partials[blockIdx.x].dtc = dtc;
+        m.partials[blockIdx.x].dth = dth;
+        __threadfence();
+        const unsigned ticket = atomicAdd(&m.result->blocks_done, 1u);
+        last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double a = 1.0e+20, b = 1.0e+20;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+        a = fmin(a, __ldcg(&m.partials[k].dtc));
+        b = fmin(b, __ldcg(&m.partials[k].dth));
+    }
+    __syncthreads();  // block_min2's shared scratch is reused
+    block_min2(a, b);
+    if (threadIdx.x == 0) {
+        m.result->dtcourant = a;
+        m.result->dthydro = b;
+        m.result->blocks_done = 0u;
+    }
+}
+
+// --- node update ------------------------------------------------------------
+
+// Acceleration, symmetry-plane zeroing, velocity with u_cut and position of
+// node n from its gathered force (lulesh.cc:1115-1158, 566-588).
+__device__ __forceinline__ void node_update(const Mesh& m, int n, double fx, double fy, double fz,
+                                            double dt) {
+    m.fx[n] = fx;
+    m.fy[n] = fy;
+    m.fz[n] = fz;
+    const double mass = LD(m.nodalMass + n);
+    double ax = fx / mass, ay = fy / mass, az = fz / mass;
+    const unsigned sym = LD(m.nodeSymm + n);
+    if (sym & 1u) ax = 0.0;
+    if (sym & 2u) ay = 0.0;
+    if (sym & 4u) az = 0.0;
+    m.xdd[n] = ax;
+    m.ydd[n] = ay;
+    m.zdd[n] = az;
+    const double u_cut = m.prm.u_cut;
+    double vx = m.xd[n] + ax * dt;
+    if (fabs(vx) < u_cut) vx = 0.0;
+    double vy = m.yd[n] + ay * dt;
+    if (fabs(vy) < u_cut) vy = 0.0;
+    double vz = m.zd[n] + az * dt;
+    if (fabs(vz) < u_cut) vz = 0.0;
+    m.xd[n] = vx;
+    m.yd[n] = vy;
+    m.zd[n] = vz;
+    m.x[n] = m.x[n] + vx * dt;
+    m.y[n] = m.y[n] + vy * dt;
+    m.z[n] = m.z[n] + vz * dt;
+}
+
+// CheckAndUpdateVolumeForElems (lulesh.cc:1252-1272): checks the old v, then
+// stores vnew snapped to 1 within v_cut.
+__device__ __forceinline__ void update_volume(const Mesh& m, int i, double vold, double relv) {
+    const lulesh_params& P = m.prm;
+    double vc = vold;
+    if (P.eosvmin != 0.0 && vc < P.eosvmin) vc = P.eosvmin;
+    if (P.eosvmax != 0.0 && vc > P.eosvmax) vc = P.eosvmax;
+    if (vc < 0.0) raise_error(m.result, i, PHASE_KINEMATICS);
+    double vn = relv;
+    if (fabs(vn - 1.0) < P.v_cut) vn = 1.0;
+    m.v[i] = vn;
+}
+
+}  // namespace LULESH_VARIANT
+}  // namespace lulesh

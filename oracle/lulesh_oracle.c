@@ -28,6 +28,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -87,6 +88,52 @@ struct lo_domain {
 };
 
 static int g_threads = 0;
+static int g_cbrt_mode = 0;
+
+/* Cube root of the hourglass coefficient. Mode 0 is libm cbrt, as the
+ * reference (lulesh.cc:1068). Mode 1 is a cube root built from IEEE add,
+ * multiply and divide only (exponent split x = m 2^(3k), m in [1,8);
+ * least-squares quadratic start on [1,8]; four Halley steps
+ * y <- y (y^3 + 2m) / (2y^3 + m); exact rescale by 2^k), the same steps the
+ * GPU's LULESH_FP64_EXACT path takes, so the two agree bit for bit. */
+static double portable_cbrt(double x) {
+    if (!(x > 0.0)) {
+        if (x < 0.0) return -portable_cbrt(-x);
+        return x;
+    }
+    uint64_t bits;
+    memcpy(&bits, &x, sizeof bits);
+    int ex = (int)((bits >> 52) & 0x7ff);
+    if (ex == 0x7ff) return x;
+    if (ex == 0) return portable_cbrt(x * 18014398509481984.0) * 3.814697265625e-06;
+    int e = ex - 1023;
+    int k = (e >= 0) ? e / 3 : -((2 - e) / 3);
+    int r = e - 3 * k;
+    uint64_t mb = (bits & 0x000fffffffffffffULL) | ((uint64_t)(1023 + r) << 52);
+    double m;
+    memcpy(&m, &mb, sizeof m);
+    double y = 0.8209 + m * (0.2374 - m * 0.01159);
+    for (int it = 0; it < 4; ++it) {
+        double y3 = y * y * y;
+        y = y * (y3 + 2.0 * m) / (2.0 * y3 + m);
+    }
+    /* Newton correction with an error-free residual y^3 - m */
+    double t = y * y;
+    double e1 = fma(y, y, -t);
+    double u = t * y;
+    double e2 = fma(t, y, -u);
+    double res = (u - m) + (e2 + e1 * y);
+    y = y - res / (3.0 * t);
+    uint64_t sb = (uint64_t)(1023 + k) << 52;
+    double scale;
+    memcpy(&scale, &sb, sizeof scale);
+    return y * scale;
+}
+
+void lo_set_cbrt_mode(int mode) { g_cbrt_mode = mode; }
+double lo_portable_cbrt(double x) { return portable_cbrt(x); }
+
+static inline double hg_cbrt(double x) { return g_cbrt_mode ? portable_cbrt(x) : cbrt(x); }
 
 void lo_set_threads(int n) {
     g_threads = n;
@@ -364,7 +411,7 @@ static int phase_forces(lo_domain* d) {
             for (int k = 0; k < 8; ++k)
                 hg[k][m] = g[k] - volinv * (dvdx[k] * hx + dvdy[k] * hy + dvdz[k] * hz);
         }
-        double coefficient = -hgcoef * 0.01 * d->ss[i] * d->elemMass[i] / cbrt(determ);
+        double coefficient = -hgcoef * 0.01 * d->ss[i] * d->elemMass[i] / hg_cbrt(determ);
         double vel[8];
         double* outs[3] = {d->fx_hg, d->fy_hg, d->fz_hg};
         const double* vsrc[3] = {d->xd, d->yd, d->zd};

@@ -29,6 +29,11 @@ typedef struct lo_domain lo_domain;
 lo_domain* lo_create(int s, int nr, int balance, int cost, double energy_scale);
 void lo_destroy(lo_domain* d);
 
+/* Cube root used for the hourglass coefficient: 0 = libm cbrt (the
+ * reference), 1 = the portable IEEE-only cube root of the GPU's exact path. */
+void lo_set_cbrt_mode(int mode);
+double lo_portable_cbrt(double x);
+
 /* Worker threads for the element/node loops (OpenMP builds only). */
 void lo_set_threads(int n);
 int lo_get_threads(void);
