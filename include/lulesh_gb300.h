@@ -197,6 +197,26 @@ typedef struct lulesh_profile {
 int lulesh_dev_profile_begin(lulesh_dev* dev);
 int lulesh_dev_profile_end(lulesh_dev* dev, lulesh_profile* out);
 
+/* Courant and hydro time-step constraints without allocating device memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc, such as a host framework that owns every device allocation
+ * through its own pool or budget, or a loop that cannot afford cudaMalloc's
+ * possible device-wide synchronization. From the caller's device arrays ss,
+ * vdov and arealg (numElem each) it writes out_dt[0] = dtcourant and
+ * out_dt[1] = dthydro (out_dt: 2 doubles of device memory) with the minima
+ * lulesh_dev_step returns, using qqc and dvovmax of lulesh_params.
+ * Asynchronous on `stream` (a cudaStream_t; NULL = the legacy default stream).
+ * Working memory is one file-scope device array of 256 KiB that every GPU
+ * loading this library keeps until exit; it bounds numElem to
+ * LULESH_NOALLOC_MAX_ELEMS and larger sizes return LULESH_EINVAL. The first
+ * call on a device looks up that array's device address once (call it before
+ * any stream capture). Calls share the array: calls whose kernels overlap on
+ * the GPU race and must be serialized by the caller. */
+#define LULESH_NOALLOC_MAX_ELEMS 4194304
+int lulesh_dt_constraints_noalloc(const double* ss, const double* vdov, const double* arealg,
+                                  int32_t numElem, double qqc, double dvovmax, double* out_dt,
+                                  void* stream);
+
 /* Page-locks (pin = 1) or releases (pin = 0) the host arrays of a Domain so
  * lulesh_leapfrog's per-cycle copies run at full link bandwidth. */
 int lulesh_domain_pin(lulesh_domain* d, int32_t pin);

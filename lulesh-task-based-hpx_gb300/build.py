@@ -39,6 +39,7 @@ UNITS = [
     ("mixed.cu", []),
     ("time_increment.cu", ["--fmad=false"]),
     ("capi.cu", []),
+    ("noalloc.cu", []),
     ("domain.cpp", ["-x", "cu", "--fmad=false"]),
 ]
 

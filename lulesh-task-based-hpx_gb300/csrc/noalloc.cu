@@ -1,0 +1,115 @@
+// Allocation-free Courant/hydro time-step constraints.
+//
+// lulesh_dt_constraints_noalloc computes the same two minima as the dt part of
+// the material kernel (the reference's CalcConstraintForElemsTask), from
+// caller-owned device arrays, for callers that cannot allocate device memory:
+// a host framework that owns every device allocation through its own pool or
+// budget, or a loop that cannot afford cudaMalloc/cudaFree, which may
+// synchronize the whole device. Its only working memory is the file-scope
+// array below, which every GPU that loads this library holds until exit.
+//
+// The reduction needs one partial minimum per thread block plus an arrival
+// counter, so the array holds kNoAllocMaxBlocks partials (256 KiB) and the
+// counter: at 256 threads per block that bounds numElem to
+// LULESH_NOALLOC_MAX_ELEMS = 4,194,304 (an s = 161 cube); larger sizes are
+// rejected with LULESH_EINVAL.
+//
+// All calls share that one array. Each call clears the counter on its stream
+// before its kernel, and the kernel leaves the partials of the last call
+// behind; two calls whose kernels overlap on the GPU (different streams, or
+// different host threads on one device) race on the array and give wrong
+// minima, so serialize them.
+#define LULESH_VARIANT noalloc
+#define LULESH_EXACT 0
+#include <mutex>
+
+#include "step_math.cuh"
+
+namespace lulesh {
+namespace noalloc {
+
+constexpr int kBlock = 256;
+constexpr int kNoAllocMaxBlocks = 16384;
+static_assert(size_t(kNoAllocMaxBlocks) * kBlock == LULESH_NOALLOC_MAX_ELEMS, "limit mismatch");
+
+// partials [0, kNoAllocMaxBlocks) then the arrival counter
+constexpr size_t kCounterOffset = sizeof(DtPartial) * kNoAllocMaxBlocks;
+constexpr size_t kScratchBytes = kCounterOffset + 256;
+
+static __device__ __align__(256) unsigned char g_dt_scratch[kScratchBytes];
+
+__global__ void __launch_bounds__(kBlock)
+    k_dt_constraints(const double* __restrict__ ss, const double* __restrict__ vdov,
+                     const double* __restrict__ arealg, int n, lulesh_params prm,
+                     unsigned char* scratch, double* out) {
+    DtPartial* partials = reinterpret_cast<DtPartial*>(scratch);
+    unsigned* counter = reinterpret_cast<unsigned*>(scratch + kCounterOffset);
+    double dtc = 1.0e+20, dth = 1.0e+20;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dt_constraints(prm, __ldg(ss + i), __ldg(vdov + i), __ldg(arealg + i), dtc, dth);
+    block_min2(dtc, dth);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x].dtc = dtc;
+        partials[blockIdx.x].dth = dth;
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double a = 1.0e+20, b = 1.0e+20;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+        a = fmin(a, __ldcg(&partials[k].dtc));
+        b = fmin(b, __ldcg(&partials[k].dth));
+    }
+    __syncthreads();
+    block_min2(a, b);
+    if (threadIdx.x == 0) {
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
+// Device address of g_dt_scratch for each device, looked up once per device
+// (with that device current) on the first call there.
+static std::mutex g_mutex;
+static void* g_addr[64] = {};
+
+static int scratch_address(int device, void** out) {
+    if (device < 0 || device >= 64) return LULESH_EINVAL;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_addr[device]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_dt_scratch) != cudaSuccess || !p) return LULESH_ECUDA;
+        g_addr[device] = p;
+    }
+    *out = g_addr[device];
+    return LULESH_OK;
+}
+
+}  // namespace noalloc
+}  // namespace lulesh
+
+extern "C" int lulesh_dt_constraints_noalloc(const double* ss, const double* vdov,
+                                             const double* arealg, int32_t numElem, double qqc,
+                                             double dvovmax, double* out_dt, void* stream) {
+    using namespace lulesh::noalloc;
+    if (!ss || !vdov || !arealg || !out_dt || numElem < 1) return LULESH_EINVAL;
+    if (numElem > LULESH_NOALLOC_MAX_ELEMS) return LULESH_EINVAL;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return LULESH_ECUDA;
+    void* base = nullptr;
+    const int st = scratch_address(device, &base);
+    if (st != LULESH_OK) return st;
+    unsigned char* scratch = static_cast<unsigned char*>(base);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(scratch + kCounterOffset, 0, sizeof(unsigned), s) != cudaSuccess)
+        return LULESH_ECUDA;
+    lulesh_params prm{};
+    prm.qqc = qqc;
+    prm.dvovmax = dvovmax;
+    const int blocks = (numElem + kBlock - 1) / kBlock;
+    k_dt_constraints<<<blocks, kBlock, 0, s>>>(ss, vdov, arealg, numElem, prm, scratch, out_dt);
+    return cudaGetLastError() == cudaSuccess ? LULESH_OK : LULESH_ECUDA;
+}
