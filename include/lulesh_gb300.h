@@ -221,6 +221,12 @@ int lulesh_dt_constraints_noalloc(const double* ss, const double* vdov, const do
  * lulesh_leapfrog's per-cycle copies run at full link bandwidth. */
 int lulesh_domain_pin(lulesh_domain* d, int32_t pin);
 
+/* Measures the current GPU's pipe rates (no counterpart in the reference):
+ * out[0] double FMA/s, out[1] double add/s, out[2] double divide/s,
+ * out[3] double square root/s, out[4] float FMA/s (per-thread operations).
+ * The double path is bound by out[0]; takes about 50 ms. */
+int lulesh_probe_pipe_rates(double out[5]);
+
 /* Selects the CUDA device used by handles created afterwards on this thread. */
 int lulesh_set_device(int32_t device);
 

@@ -115,6 +115,7 @@ def library() -> C.CDLL:
         "lulesh_dev_profile_end": (i32, [vp, C.POINTER(Profile)]),
         "lulesh_domain_pin": (i32, [vp, i32]),
         "lulesh_set_device": (i32, [i32]),
+        "lulesh_probe_pipe_rates": (i32, [C.POINTER(dbl)]),
         "lulesh_cbrt_portable": (dbl, [dbl]),
         "lulesh_strerror": (C.c_char_p, [i32]),
     }
@@ -292,3 +293,10 @@ def cbrt_portable(x: float) -> float:
 
 def set_device(device: int) -> None:
     _check(library().lulesh_set_device(device), "lulesh_set_device")
+
+
+def pipe_rates() -> dict:
+    """Measured double FMA/add/divide/sqrt and float FMA rates (ops/s) of the current GPU."""
+    out = (C.c_double * 5)()
+    _check(library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
+    return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma"), list(out)))

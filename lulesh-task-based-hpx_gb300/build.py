@@ -40,6 +40,7 @@ UNITS = [
     ("time_increment.cu", ["--fmad=false"]),
     ("capi.cu", []),
     ("noalloc.cu", []),
+    ("probe.cu", []),
     ("domain.cpp", ["-x", "cu", "--fmad=false"]),
 ]
 
