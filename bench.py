@@ -57,6 +57,9 @@ BYTES_PER_UNIT = {
     "fp64": {"forces": 512, "nodes": 573, "kinematics": 184, "material": 204},
     "mixed": {"forces": 224, "nodes": 333, "kinematics": 184, "material": 180},
 }
+# DRAM bytes (read + write) per unit measured by ncu at s=100, where every
+# array exceeds L2 (profiles/dram_traffic_s100.md); scaled by units per launch.
+TRAFFIC_PER_UNIT = {"fp64": {"forces": 455, "nodes": 549, "kinematics": 141, "material": 183}}
 # Algorithmic double-precision operations per unit (adds, multiplies,
 # divides, square and cube roots each counted once), from counting the
 # reference's arithmetic at s=30 r=11; the material kernel adds 68 per EOS pass.
@@ -200,9 +203,12 @@ def roofline(prof: dict, precision: str, ne: int, nn: int, rep_avg: float,
     else:
         flops = FLOPS_PER_UNIT[dom]
     tflops = flops * units / avg_s / 1e12
+    tpu = TRAFFIC_PER_UNIT.get(precision, {}).get(dom)
     return {
         "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
-        "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+        "unit": "GB/s", "frac": round(achieved / peak, 4),
+        "traffic": tpu * units if tpu else None,
+        "traffic_note": "ncu dram bytes per unit at s=100 x units per launch" if tpu else None,
         "peak_kind": f"{kind} ({'MEASURED_PEAKS.json hbm_gbs' if kind == 'measured' else 'recipe fallback'})",
         "bytes_per_launch": bytes_launch, "avg_launch_ms": round(km[dom] / cyc, 4),
         "kernel_share": {k: round(v / max(sum(km.values()), 1e-30), 4) for k, v in km.items()},
