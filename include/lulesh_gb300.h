@@ -164,6 +164,67 @@ int lulesh_dev_run(lulesh_dev* dev, lulesh_time_state* ts, int32_t max_cycles, i
 int lulesh_dev_run_graph(lulesh_dev* dev, lulesh_time_state* ts, int32_t max_cycles,
                          int32_t sync_every, int32_t* cycles_run);
 
+/* ---------------- batched ensembles ---------------------------------------------------
+ * No counterpart in the reference, which runs one problem per process. A
+ * batch keeps many independent Sedov problems resident in one device pool;
+ * each cycle of every active problem runs in one CUDA graph: a device-side
+ * TimeIncrement per problem, then the four phases as persistent launches
+ * over an (instance, tile) work queue, then the dt hand-off. Each problem
+ * keeps its own dt, stoptime and cycle limit; problems join (admit) and
+ * leave (retire) between graph replays without re-capturing the graph. */
+typedef struct lulesh_batch lulesh_batch;
+
+typedef struct lulesh_problem {
+    int32_t s, nr, balance, cost; /* --s --r --b --c */
+    double energy_scale;          /* deposited energy multiplier (1.0 = the reference) */
+    double stoptime;              /* <= 0: the reference's 1e-2 */
+    int32_t max_cycles;           /* <= 0: no cycle limit (the reference's --i default) */
+    int32_t pad_;
+} lulesh_problem;
+
+typedef struct lulesh_slot_status {
+    int32_t in_use, active, cycle, err; /* err: 0 or LULESH_EVOLUME */
+    int32_t err_elem, numElem, s, pad_;
+    double time, deltatime, dtcourant, dthydro;
+} lulesh_slot_status;
+
+/* Per-phase launch shapes of the persistent kernels (forces, nodes,
+ * kinematics, material) and the tile size in units. */
+typedef struct lulesh_batch_tuning {
+    int32_t block[4];
+    int32_t blocks_per_sm[4];
+    int32_t tile;
+    int32_t pad_;
+    double ms_per_cycle; /* measured by lulesh_batch_autotune */
+} lulesh_batch_tuning;
+
+/* pool_bytes of device memory hold the problems' arrays; at most max_slots
+ * problems at once. */
+int lulesh_batch_create(int32_t precision, uint64_t pool_bytes, int32_t max_slots, lulesh_batch** out);
+void lulesh_batch_destroy(lulesh_batch* b);
+/* Device bytes one s^3 problem takes in a pool of this precision. */
+int lulesh_batch_footprint(int32_t precision, int32_t s, uint64_t* bytes);
+/* Builds the problem (Domain::Domain on the host), copies it into the pool
+ * and makes it active. LULESH_ENOMEM when the pool or the slots are full. */
+int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot);
+/* Frees a slot (finished or not) and its pool memory. */
+int lulesh_batch_retire(lulesh_batch* b, int32_t slot);
+/* Replays the cycle graph `cycles` times, then refreshes the slot status.
+ * *active_slots (optional) = slots still running; *device_ms (optional) =
+ * device time of the replays. */
+int lulesh_batch_run(lulesh_batch* b, int32_t cycles, int32_t* active_slots, double* device_ms);
+int lulesh_batch_status(const lulesh_batch* b, lulesh_slot_status* out, int32_t n);
+/* Copies fields of one slot into a host view of the same problem size. */
+int lulesh_batch_download(lulesh_batch* b, int32_t slot, lulesh_domain_view* host, uint32_t mask);
+/* Times candidate launch shapes and tile sizes on the resident problems
+ * (their state is saved first and restored after, so tuning does not
+ * advance them), keeps the fastest and reports it. */
+int lulesh_batch_autotune(lulesh_batch* b, int32_t cycles_per_candidate, lulesh_batch_tuning* chosen);
+int lulesh_batch_get_tuning(const lulesh_batch* b, lulesh_batch_tuning* out);
+int lulesh_batch_set_tuning(lulesh_batch* b, const lulesh_batch_tuning* t);
+/* Kernel launches issued so far (graph replays count every kernel node). */
+int64_t lulesh_batch_launch_count(const lulesh_batch* b);
+
 /* Test hooks (no counterpart in the reference; they expose the step's
  * intermediate arrays so each kernel can be checked on its own). */
 #define LULESH_PHASE_FORCES 0     /* stress + hourglass corner forces */

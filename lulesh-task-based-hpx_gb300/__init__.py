@@ -66,6 +66,23 @@ class Profile(C.Structure):
 KERNELS = ("forces", "nodes", "kinematics", "material")
 
 
+class Problem(C.Structure):
+    _fields_ = [("s", C.c_int32), ("nr", C.c_int32), ("balance", C.c_int32), ("cost", C.c_int32),
+                ("energy_scale", C.c_double), ("stoptime", C.c_double), ("max_cycles", C.c_int32),
+                ("pad_", C.c_int32)]
+
+
+class SlotStatus(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("in_use", "active", "cycle", "err", "err_elem", "numElem", "s",
+                                          "pad_")] + \
+               [(n, C.c_double) for n in ("time", "deltatime", "dtcourant", "dthydro")]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("block", C.c_int32 * 4), ("blocks_per_sm", C.c_int32 * 4), ("tile", C.c_int32),
+                ("pad_", C.c_int32), ("ms_per_cycle", C.c_double)]
+
+
 class DomainView(C.Structure):
     _fields_ = (
         [(n, C.c_int32) for n in ("numElem", "numNode", "sizeX", "numReg", "cost", "numSymmX",
@@ -116,6 +133,18 @@ def library() -> C.CDLL:
         "lulesh_domain_pin": (i32, [vp, i32]),
         "lulesh_set_device": (i32, [i32]),
         "lulesh_probe_pipe_rates": (i32, [C.POINTER(dbl)]),
+        "lulesh_batch_create": (i32, [i32, C.c_uint64, i32, C.POINTER(vp)]),
+        "lulesh_batch_destroy": (None, [vp]),
+        "lulesh_batch_footprint": (i32, [i32, i32, C.POINTER(C.c_uint64)]),
+        "lulesh_batch_admit": (i32, [vp, C.POINTER(Problem), C.POINTER(i32)]),
+        "lulesh_batch_retire": (i32, [vp, i32]),
+        "lulesh_batch_run": (i32, [vp, i32, C.POINTER(i32), C.POINTER(dbl)]),
+        "lulesh_batch_status": (i32, [vp, C.POINTER(SlotStatus), i32]),
+        "lulesh_batch_download": (i32, [vp, i32, C.POINTER(DomainView), u32]),
+        "lulesh_batch_autotune": (i32, [vp, i32, C.POINTER(BatchTuning)]),
+        "lulesh_batch_get_tuning": (i32, [vp, C.POINTER(BatchTuning)]),
+        "lulesh_batch_set_tuning": (i32, [vp, C.POINTER(BatchTuning)]),
+        "lulesh_batch_launch_count": (i64, [vp]),
         "lulesh_cbrt_portable": (dbl, [dbl]),
         "lulesh_strerror": (C.c_char_p, [i32]),
     }
@@ -300,3 +329,107 @@ def pipe_rates() -> dict:
     out = (C.c_double * 5)()
     _check(library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
     return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma"), list(out)))
+
+
+def _tuning_dict(t: BatchTuning) -> dict:
+    return {"block": list(t.block), "blocks_per_sm": list(t.blocks_per_sm), "tile": t.tile,
+            "ms_per_cycle": t.ms_per_cycle}
+
+
+class Batch:
+    """A device pool of independent Sedov problems, one CUDA graph per cycle.
+
+    Problems are admitted into slots (each built by Domain::Domain's set-up,
+    optionally with a scaled deposit, its own stoptime and cycle limit), all
+    active slots advance together with run(), and finished slots are retired
+    to free their pool memory.
+    """
+
+    def __init__(self, precision: str = "fp64", pool_bytes: int = 8 << 30, max_slots: int = 64):
+        lib = library()
+        h = C.c_void_p()
+        _check(lib.lulesh_batch_create(PRECISION[precision], pool_bytes, max_slots, C.byref(h)),
+               "lulesh_batch_create")
+        self._h = h
+        self._lib = lib
+        self.precision = precision
+        self.max_slots = max_slots
+        self.specs: dict[int, dict] = {}
+
+    @staticmethod
+    def footprint(precision: str, s: int) -> int:
+        out = C.c_uint64()
+        _check(library().lulesh_batch_footprint(PRECISION[precision], s, C.byref(out)),
+               "lulesh_batch_footprint")
+        return out.value
+
+    def admit(self, s: int, nr: int = 11, balance: int = 1, cost: int = 1, energy_scale: float = 1.0,
+              stoptime: float = 0.0, max_cycles: int = 0) -> int:
+        p = Problem(s, nr, balance, cost, energy_scale, stoptime, max_cycles, 0)
+        slot = C.c_int32()
+        _check(self._lib.lulesh_batch_admit(self._h, C.byref(p), C.byref(slot)), "lulesh_batch_admit")
+        self.specs[slot.value] = {"s": s, "nr": nr, "balance": balance, "cost": cost,
+                                  "energy_scale": energy_scale}
+        return slot.value
+
+    def try_admit(self, **kw) -> int | None:
+        """admit(), or None when the pool or the slots are full."""
+        try:
+            return self.admit(**kw)
+        except LuleshError as e:
+            if e.status == ENOMEM:
+                return None
+            raise
+
+    def retire(self, slot: int) -> None:
+        _check(self._lib.lulesh_batch_retire(self._h, slot), "lulesh_batch_retire")
+        self.specs.pop(slot, None)
+
+    def run(self, cycles: int) -> tuple[int, float]:
+        """Replays `cycles` cycles; returns (slots still active, device ms)."""
+        active, ms = C.c_int32(), C.c_double()
+        _check(self._lib.lulesh_batch_run(self._h, cycles, C.byref(active), C.byref(ms)),
+               "lulesh_batch_run")
+        return active.value, ms.value
+
+    def status(self) -> list[dict]:
+        arr = (SlotStatus * self.max_slots)()
+        _check(self._lib.lulesh_batch_status(self._h, arr, self.max_slots), "lulesh_batch_status")
+        out = []
+        for i, st in enumerate(arr):
+            if st.in_use:
+                out.append({"slot": i, **{k: getattr(st, k) for k, _ in SlotStatus._fields_ if k != "pad_"}})
+        return out
+
+    def download(self, slot: int, mask: int = F_ALL) -> HostDomain:
+        """Fields of a slot, in a fresh HostDomain of the same problem."""
+        sp = self.specs[slot]
+        dom = HostDomain(sp["s"], sp["nr"], sp["balance"], sp["cost"], sp["energy_scale"])
+        _check(self._lib.lulesh_batch_download(self._h, slot, dom.view_ptr, mask), "lulesh_batch_download")
+        return dom
+
+    def autotune(self, cycles: int = 2) -> dict:
+        t = BatchTuning()
+        _check(self._lib.lulesh_batch_autotune(self._h, cycles, C.byref(t)), "lulesh_batch_autotune")
+        return _tuning_dict(t)
+
+    def tuning(self) -> dict:
+        t = BatchTuning()
+        _check(self._lib.lulesh_batch_get_tuning(self._h, C.byref(t)), "lulesh_batch_get_tuning")
+        return _tuning_dict(t)
+
+    def set_tuning(self, block, blocks_per_sm, tile: int) -> None:
+        t = BatchTuning((C.c_int32 * 4)(*block), (C.c_int32 * 4)(*blocks_per_sm), tile, 0, 0.0)
+        _check(self._lib.lulesh_batch_set_tuning(self._h, C.byref(t)), "lulesh_batch_set_tuning")
+
+    @property
+    def launches(self) -> int:
+        return self._lib.lulesh_batch_launch_count(self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lulesh_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

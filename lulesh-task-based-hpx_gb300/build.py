@@ -41,6 +41,7 @@ UNITS = [
     ("capi.cu", []),
     ("noalloc.cu", []),
     ("probe.cu", []),
+    ("batch.cu", []),
     ("domain.cpp", ["-x", "cu", "--fmad=false"]),
 ]
 

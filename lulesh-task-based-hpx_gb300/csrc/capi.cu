@@ -90,7 +90,7 @@ struct lulesh_dev {
 
 namespace {
 
-int validate_view(const lulesh_domain_view* v) {
+int check_view(const lulesh_domain_view* v) {
     if (!v || v->numElem < 1 || v->numNode < 8 || v->numReg < 1 || v->cost < 0) return LULESH_EINVAL;
     if ((int64_t)v->numElem * 8 > INT32_MAX) return LULESH_EINVAL;
     const void* req[] = {v->x, v->y, v->z, v->xd, v->yd, v->zd, v->xdd, v->ydd, v->zdd, v->fx,
@@ -126,11 +126,9 @@ int validate_view(const lulesh_domain_view* v) {
     return LULESH_OK;
 }
 
-// Lays out every device array of the handle in the arena; with base == null
-// it only measures.
-void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
-    Mesh& m = d->m;
-    const bool mixed = d->precision == LULESH_MIXED;
+// Lays out the mesh arrays of one problem in the arena; with base == null it
+// only measures.
+void carve_mesh(Mesh& m, Arena& a, bool mixed, int ne, int nn) {
     for (double** f : {&m.x, &m.y, &m.z, &m.xd, &m.yd, &m.zd, &m.xdd, &m.ydd, &m.zdd, &m.fx, &m.fy,
                        &m.fz})
         *f = a.take<double>(nn);
@@ -159,6 +157,13 @@ void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
         for (double** f : {&m.dvxi, &m.dveta, &m.dvzeta, &m.dxxi, &m.dxeta, &m.dxzeta})
             *f = a.take<double>(ne);
     }
+}
+
+// Every device array of a single-problem handle: the mesh, then the
+// reduction scratch and the graph form's time state.
+void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
+    Mesh& m = d->m;
+    carve_mesh(m, a, d->precision == LULESH_MIXED, ne, nn);
     m.partials = a.take<lulesh::DtPartial>(matGrid);
     m.result = a.take<StepResult>(1);
     d->d_time = a.take<DevTime>(1);
@@ -171,8 +176,7 @@ struct Copy {
 };
 
 // The (device, host) pairs of the field groups in `mask`.
-std::vector<Copy> groups(const lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask) {
-    const Mesh& m = d->m;
+std::vector<Copy> groups(const Mesh& m, const lulesh_domain_view* v, uint32_t mask) {
     const size_t nb = sizeof(double) * size_t(m.numNode), eb = sizeof(double) * size_t(m.numElem);
     std::vector<Copy> c;
     if (mask & LULESH_F_POS) c.insert(c.end(), {{m.x, v->x, nb}, {m.y, v->y, nb}, {m.z, v->z, nb}});
@@ -189,6 +193,53 @@ std::vector<Copy> groups(const lulesh_dev* d, const lulesh_domain_view* v, uint3
                            {m.arealg, v->arealg, eb}});
     if (mask & LULESH_F_SS) c.push_back({m.ss, v->ss, eb});
     return c;
+}
+
+// Uploads topology, derived per-node/per-element arrays and the whole
+// mutable state of v into the carved mesh m, refreshes the mixed path's
+// float-pair mirrors, and waits for the copies (some read host vectors that
+// live only in this call).
+int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaStream_t s) {
+    const int ne = v->numElem, nn = v->numNode;
+    // per-node symmetry bits, per-element EOS repeat count and the
+    // repeat-count grouping of the material phase
+    std::vector<uint8_t> symm(nn, 0);
+    for (int k = 0; k < v->numSymmX; ++k) symm[v->symmX[k]] |= 1;
+    for (int k = 0; k < v->numSymmY; ++k) symm[v->symmY[k]] |= 2;
+    for (int k = 0; k < v->numSymmZ; ++k) symm[v->symmZ[k]] |= 4;
+    std::vector<int32_t> rep(ne), order(ne);
+    for (int i = 0; i < ne; ++i) rep[i] = region_rep(v->regNumList[i] - 1, v->numReg, v->cost);
+    for (int i = 0; i < ne; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rep[a] > rep[b]; });
+
+    const size_t eb = sizeof(int32_t) * size_t(ne);
+    const Copy consts[] = {
+        {const_cast<double*>(m.nodalMass), v->nodalMass, sizeof(double) * size_t(nn)},
+        {const_cast<uint8_t*>(m.nodeSymm), symm.data(), size_t(nn)},
+        {const_cast<int32_t*>(m.nodelist), v->nodelist, 8 * eb},
+        {const_cast<int32_t*>(m.lxim), v->lxim, eb},
+        {const_cast<int32_t*>(m.lxip), v->lxip, eb},
+        {const_cast<int32_t*>(m.letam), v->letam, eb},
+        {const_cast<int32_t*>(m.letap), v->letap, eb},
+        {const_cast<int32_t*>(m.lzetam), v->lzetam, eb},
+        {const_cast<int32_t*>(m.lzetap), v->lzetap, eb},
+        {const_cast<int32_t*>(m.elemBC), v->elemBC, eb},
+        {const_cast<double*>(m.volo), v->volo, sizeof(double) * size_t(ne)},
+        {const_cast<double*>(m.elemMass), v->elemMass, sizeof(double) * size_t(ne)},
+        {const_cast<int32_t*>(m.nodeElemStart), v->nodeElemStart, sizeof(int32_t) * (size_t(nn) + 1)},
+        {const_cast<int32_t*>(m.nodeElemCornerList), v->nodeElemCornerList, 8 * eb},
+        {const_cast<int32_t*>(m.matOrder), order.data(), eb},
+        {const_cast<int32_t*>(m.elemRep), rep.data(), eb},
+    };
+    for (const Copy& c : consts) CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, s));
+    for (const Copy& c : groups(m, v, LULESH_F_ALL))
+        CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, s));
+    if (precision == LULESH_MIXED) {
+        lulesh::mixed::launch_mirror(m, s);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(s));
+    return LULESH_OK;
 }
 
 int run_cycle(lulesh_dev* d, double dt) {
@@ -256,7 +307,7 @@ int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev
     *out = nullptr;
     if (precision != LULESH_FP64 && precision != LULESH_FP64_EXACT && precision != LULESH_MIXED)
         return LULESH_EINVAL;
-    int st = validate_view(v);
+    int st = check_view(v);
     if (st != LULESH_OK) return st;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LULESH_ENODEV;
@@ -265,17 +316,6 @@ int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
 
     const int ne = v->numElem, nn = v->numNode;
-    // derived host arrays: per-node symmetry bits, per-element EOS repeat
-    // count and the repeat-count grouping of the material kernel
-    std::vector<uint8_t> symm(nn, 0);
-    for (int k = 0; k < v->numSymmX; ++k) symm[v->symmX[k]] |= 1;
-    for (int k = 0; k < v->numSymmY; ++k) symm[v->symmY[k]] |= 2;
-    for (int k = 0; k < v->numSymmZ; ++k) symm[v->symmZ[k]] |= 4;
-    std::vector<int32_t> rep(ne), order(ne);
-    for (int i = 0; i < ne; ++i) rep[i] = region_rep(v->regNumList[i] - 1, v->numReg, v->cost);
-    for (int i = 0; i < ne; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rep[a] > rep[b]; });
-
     lulesh_dev* d = new (std::nothrow) lulesh_dev;
     if (!d) return LULESH_ENOMEM;
     d->precision = precision;
@@ -303,34 +343,11 @@ int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev
     if (cudaMallocHost(&d->h_result, sizeof(StepResult)) != cudaSuccess) return fail(LULESH_ENOMEM);
     if (cudaMallocHost(&d->h_time, sizeof(DevTime)) != cudaSuccess) return fail(LULESH_ENOMEM);
 
-    const size_t eb = sizeof(int32_t) * size_t(ne);
-    const Copy consts[] = {
-        {const_cast<double*>(m.nodalMass), v->nodalMass, sizeof(double) * size_t(nn)},
-        {const_cast<uint8_t*>(m.nodeSymm), symm.data(), size_t(nn)},
-        {const_cast<int32_t*>(m.nodelist), v->nodelist, 8 * eb},
-        {const_cast<int32_t*>(m.lxim), v->lxim, eb},
-        {const_cast<int32_t*>(m.lxip), v->lxip, eb},
-        {const_cast<int32_t*>(m.letam), v->letam, eb},
-        {const_cast<int32_t*>(m.letap), v->letap, eb},
-        {const_cast<int32_t*>(m.lzetam), v->lzetam, eb},
-        {const_cast<int32_t*>(m.lzetap), v->lzetap, eb},
-        {const_cast<int32_t*>(m.elemBC), v->elemBC, eb},
-        {const_cast<double*>(m.volo), v->volo, sizeof(double) * size_t(ne)},
-        {const_cast<double*>(m.elemMass), v->elemMass, sizeof(double) * size_t(ne)},
-        {const_cast<int32_t*>(m.nodeElemStart), v->nodeElemStart, sizeof(int32_t) * (size_t(nn) + 1)},
-        {const_cast<int32_t*>(m.nodeElemCornerList), v->nodeElemCornerList, 8 * eb},
-        {const_cast<int32_t*>(m.matOrder), order.data(), eb},
-        {const_cast<int32_t*>(m.elemRep), rep.data(), eb},
-    };
-    for (const Copy& c : consts)
-        if (cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, d->stream) != cudaSuccess)
-            return fail(LULESH_ECUDA);
     if (cudaMemsetAsync(m.result, 0, sizeof(StepResult), d->stream) != cudaSuccess)
         return fail(LULESH_ECUDA);
-    // the copies above read pageable host vectors that die with this scope
-    if (cudaStreamSynchronize(d->stream) != cudaSuccess) return fail(LULESH_ECUDA);
-    st = lulesh_dev_upload(d, v, LULESH_F_ALL);
+    st = upload_mesh(m, v, precision, d->stream);
     if (st != LULESH_OK) return fail(st);
+    if (precision == LULESH_MIXED) ++d->launches;  // the float-pair mirror kernel
     *out = d;
     return LULESH_OK;
 }
@@ -352,7 +369,7 @@ void lulesh_dev_destroy(lulesh_dev* d) {
 
 int lulesh_dev_upload(lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask) {
     if (!d || !v || v->numElem != d->m.numElem || v->numNode != d->m.numNode) return LULESH_EINVAL;
-    for (const Copy& c : groups(d, v, mask)) {
+    for (const Copy& c : groups(d->m, v, mask)) {
         if (!c.host) return LULESH_EINVAL;
         CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, d->stream));
     }
@@ -366,7 +383,7 @@ int lulesh_dev_upload(lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask)
 
 int lulesh_dev_download(lulesh_dev* d, lulesh_domain_view* v, uint32_t mask) {
     if (!d || !v || v->numElem != d->m.numElem || v->numNode != d->m.numNode) return LULESH_EINVAL;
-    for (const Copy& c : groups(d, v, mask)) {
+    for (const Copy& c : groups(d->m, v, mask)) {
         if (!c.host) return LULESH_EINVAL;
         CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->stream));
     }
@@ -560,3 +577,36 @@ int32_t lulesh_dev_error_elem(const lulesh_dev* d) { return d ? d->err_elem : -1
 int64_t lulesh_dev_launch_count(const lulesh_dev* d) { return d ? d->launches : 0; }
 
 }  // extern "C"
+
+namespace lulesh {
+
+int validate_view(const lulesh_domain_view* v) { return check_view(v); }
+
+size_t mesh_bytes(int precision, int numElem, int numNode) {
+    Mesh m{};
+    Arena a;
+    carve_mesh(m, a, precision == LULESH_MIXED, numElem, numNode);
+    return (a.used + 255) & ~size_t(255);
+}
+
+int mesh_init(Mesh& m, char* base, const lulesh_domain_view* v, int precision, cudaStream_t s) {
+    Arena a;
+    a.base = base;
+    carve_mesh(m, a, precision == LULESH_MIXED, v->numElem, v->numNode);
+    m.numElem = v->numElem;
+    m.numNode = v->numNode;
+    m.prm = v->params;
+    return upload_mesh(m, v, precision, s);
+}
+
+int copy_fields(const Mesh& m, const lulesh_domain_view* v, uint32_t mask, bool to_device, cudaStream_t s) {
+    for (const Copy& c : groups(m, v, mask)) {
+        if (!c.host) return LULESH_EINVAL;
+        if (to_device) CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, s));
+        else CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return LULESH_OK;
+}
+
+}  // namespace lulesh

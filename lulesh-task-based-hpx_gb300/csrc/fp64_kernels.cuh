@@ -9,12 +9,14 @@
 // fast variant lets nvcc fuse multiply-adds, which moves results by a few
 // ulps and saves FP64-pipe instructions.
 //
-// One cycle = four kernels:
-//   k_forces      element: stress + FB hourglass corner forces   (lulesh.cc:787-1113)
-//   k_nodes       node: CSR gather, a = f/m, symmetry BC, v, x    (lulesh.cc:838-862, 1115-1158, 566-588)
-//   k_kinematics  element: volume, arealg, vdov, v <- vnew, Q gradients (lulesh.cc:1169-1418)
-//   k_material    element in repeat-count order: Q limiter, EOS x rep, sound
-//                 speed, save, Courant/hydro dt minima          (lulesh.cc:1420-1974)
+// One cycle = four phases, each a per-element (or per-node) device function
+// used both by the single-problem kernels below and by the batched
+// persistent kernels of batch_kernels.cuh:
+//   forces_elem      stress + FB hourglass corner forces   (lulesh.cc:787-1113)
+//   nodes_node       CSR gather, a = f/m, symmetry BC, v, x (lulesh.cc:838-862, 1115-1158, 566-588)
+//   kinematics_elem  volume, arealg, vdov, v <- vnew, Q gradients (lulesh.cc:1169-1418)
+//   material_elem    Q limiter, EOS x rep, sound speed, save, dt constraints
+//                    (lulesh.cc:1420-1974)
 #pragma once
 
 #include "step_math.cuh"
@@ -30,13 +32,10 @@ __device__ __forceinline__ double cube_root(double x) {
 #endif
 }
 
-// Stress and hourglass corner forces of one element per thread, stored
-// separately (corner-major) so that the node gather adds them in the
-// reference's order (lulesh.cc:849-856).
-__global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m) {
-    if (m.dtime && !m.dtime->active) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.numElem) return;
+// Stress and hourglass corner forces of element i, stored separately
+// (corner-major) so that the node gather adds them in the reference's order
+// (lulesh.cc:849-856).
+__device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     const size_t N = (size_t)m.numElem;
     int nl[8];
     load_nodelist(m.nodelist, i, nl);
@@ -88,15 +87,9 @@ __global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m) {
     for (int k = 0; k < 8; ++k) m.fhz[k * N + i] = f[k];
 }
 
-// One node per thread: gather in CSR order, stress then hourglass per corner
+// Node n: gather in CSR order, stress then hourglass per corner
 // (combineVolumeForcesTaskFunc, lulesh.cc:838-862), then the node update.
-__global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
-    if (m.dtime) {
-        if (!m.dtime->active) return;
-        dt = m.dtime->deltatime;
-    }
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= m.numNode) return;
+__device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt) {
     const size_t N = (size_t)m.numElem;
     const int b = LD(m.nodeElemStart + n), e = LD(m.nodeElemStart + n + 1);
     double fx = 0.0, fy = 0.0, fz = 0.0;
@@ -114,15 +107,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
 }
 
 // CalcKinematicsForElemsTask (lulesh.cc:1169-1275) and
-// CalcMonotonicQGradientsForElemsTask (lulesh.cc:1277-1418) fused: both read
-// the same updated node positions and velocities.
-__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
-    if (m.dtime) {
-        if (!m.dtime->active) return;
-        dt = m.dtime->deltatime;
-    }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.numElem) return;
+// CalcMonotonicQGradientsForElemsTask (lulesh.cc:1277-1418) of element i:
+// both read the same updated node positions and velocities.
+__device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt) {
     int nl[8];
     load_nodelist(m.nodelist, i, nl);
     double x[8], y[8], z[8], xv[8], yv[8], zv[8];
@@ -160,29 +147,58 @@ __global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
     update_volume(m, i, vold, relv);
 }
 
-// Q limiter, EOS x rep, sound speed, save and dt minima; elements visited in
-// repeat-count order so a warp's lanes run the same number of EOS passes.
+// Material phase of the element at position t of the repeat-count order
+// (matOrder): Q limiter and q terms, rep EOS passes, sound speed and save;
+// folds its Courant and hydro constraints into dtc, dth.
+__device__ __forceinline__ void material_elem(const Mesh& m, int t, double& dtc, double& dth) {
+    const int i = LD(m.matOrder + t);
+    const double vnew = LD(m.vnew + i), vdov = LD(m.vdov + i);
+    double ql, qq;
+    q_terms<double>(m, i, m.dvxi, m.dveta, m.dvzeta, m.dxxi, m.dxeta, m.dxzeta, vnew, vdov, ql, qq);
+    m.qq[i] = qq;
+    m.ql[i] = ql;
+    double vnewc = vnew;
+    if (m.prm.eosvmin != 0.0 && vnewc < m.prm.eosvmin) vnewc = m.prm.eosvmin;
+    if (m.prm.eosvmax != 0.0 && vnewc > m.prm.eosvmax) vnewc = m.prm.eosvmax;
+    const double ss = eos_element(m, i, vnewc, LD(m.elemRep + i));
+    dt_constraints(m.prm, ss, vdov, LD(m.arealg + i), dtc, dth);
+}
+
+// --- single-problem kernels -------------------------------------------------
+
+__global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m) {
+    if (m.dtime && !m.dtime->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.numElem) forces_elem(m, i);
+}
+
+__global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
+    if (m.dtime) {
+        if (!m.dtime->active) return;
+        dt = m.dtime->deltatime;
+    }
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < m.numNode) nodes_node(m, n, dt);
+}
+
+__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
+    if (m.dtime) {
+        if (!m.dtime->active) return;
+        dt = m.dtime->deltatime;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.numElem) kinematics_elem(m, i, dt);
+}
+
+// Elements visited in repeat-count order so a warp's lanes run the same
+// number of EOS passes; the dt minima end in a last-block reduction.
 __global__ void __launch_bounds__(kMatBlock) k_material(Mesh m) {
     if (m.dtime && !m.dtime->active) return;
     double dtc = 1.0e+20, dth = 1.0e+20;  // lulesh.cc:2214-2215
-    const int N = m.numElem;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
-        const int i = LD(m.matOrder + t);
-        const double vnew = LD(m.vnew + i), vdov = LD(m.vdov + i);
-        double ql, qq;
-        q_terms<double>(m, i, m.dvxi, m.dveta, m.dvzeta, m.dxxi, m.dxeta, m.dxzeta, vnew, vdov, ql, qq);
-        m.qq[i] = qq;
-        m.ql[i] = ql;
-        double vnewc = vnew;
-        if (m.prm.eosvmin != 0.0 && vnewc < m.prm.eosvmin) vnewc = m.prm.eosvmin;
-        if (m.prm.eosvmax != 0.0 && vnewc > m.prm.eosvmax) vnewc = m.prm.eosvmax;
-        const double ss = eos_element(m, i, vnewc, LD(m.elemRep + i));
-        dt_constraints(m.prm, ss, vdov, LD(m.arealg + i), dtc, dth);
-    }
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.numElem; t += gridDim.x * blockDim.x)
+        material_elem(m, t, dtc, dth);
     finish_dt_reduction(m, dtc, dth);
 }
-
-#undef LD
 
 int launch_forces(const Mesh& m, cudaStream_t s) {
     k_forces<<<blocks_for(m.numElem, kForceBlock), kForceBlock, 0, s>>>(m);
@@ -203,3 +219,5 @@ int launch_material(const Mesh& m, cudaStream_t s) {
 
 }  // namespace LULESH_VARIANT
 }  // namespace lulesh
+
+#include "batch_kernels.cuh"

@@ -125,4 +125,66 @@ int launch_mirror(const Mesh& m, cudaStream_t s);
 int launch_time_increment(DevTime* t, StepResult* r, cudaStream_t s);
 int launch_time_finish(DevTime* t, StepResult* r, cudaStream_t s);
 
+// --- batched form -------------------------------------------------------------
+// Many independent problems ("instances"), each with its own Mesh in a slot
+// of a device pool. A phase is one persistent launch whose blocks pull
+// (instance, tile) work items from a queue; each tile is a contiguous range
+// of one instance's elements (or nodes, or positions in its matOrder).
+struct BatchTile {
+    int32_t inst;   // slot
+    int32_t first;  // first element / node / matOrder position
+    int32_t count;  // number of units
+    int32_t cost;   // units x EOS passes (material tiles), for ordering
+};
+
+enum { TILES_ELEM = 0, TILES_NODE = 1, TILES_MAT = 2 };
+
+struct BatchCtl {
+    const Mesh* meshes;   // [slots]; dtime -> times[slot], result -> results[slot]
+    DevTime* times;       // [slots]; max_cycles < 0 marks an empty slot
+    StepResult* results;  // [slots]; dt minima as atomically lowered doubles
+    const BatchTile* tiles[3];
+    const int32_t* ntiles;  // [3], in device memory so tables change without re-capture
+    unsigned* queue;        // [4] per-phase tile counters, cleared each cycle
+    int32_t slots;
+};
+
+struct BatchLaunch {
+    int32_t block;  // threads per block
+    int32_t grid;   // persistent blocks
+};
+
+constexpr int kBatchMaxBlock = 256;
+
+// Launch one batched phase; and the resident blocks per SM of a phase's
+// kernel at a block size (occupancy).
+namespace fp64 {
+int launch_batch_phase(int phase, const BatchCtl& c, const BatchLaunch& l, cudaStream_t s);
+int batch_occupancy(int phase, int block);
+}
+namespace fp64x {
+int launch_batch_phase(int phase, const BatchCtl& c, const BatchLaunch& l, cudaStream_t s);
+int batch_occupancy(int phase, int block);
+}
+namespace mixed {
+int launch_batch_phase(int phase, const BatchCtl& c, const BatchLaunch& l, cudaStream_t s);
+int batch_occupancy(int phase, int block);
+}
+
+// Per-slot TimeIncrement + dt reset, and the dt hand-off (time_increment.cu).
+int launch_batch_time_increment(const BatchCtl& c, cudaStream_t s);
+int launch_batch_time_finish(const BatchCtl& c, cudaStream_t s);
+
+// Handle-independent instance set-up shared by the single-problem handle and
+// the batch pool (capi.cu).
+size_t mesh_bytes(int precision, int numElem, int numNode);
+int validate_view(const lulesh_domain_view* v);
+// Carves the mesh arrays out of base (mesh_bytes long), uploads topology and
+// the full state of v on stream s and waits for the copies; leaves
+// partials/result/dtime/matGrid to the caller.
+int mesh_init(Mesh& m, char* base, const lulesh_domain_view* v, int precision, cudaStream_t s);
+// Copies the LULESH_F_* field groups of mask between m and v (either way)
+// on stream s and waits.
+int copy_fields(const Mesh& m, const lulesh_domain_view* v, uint32_t mask, bool to_device, cudaStream_t s);
+
 }  // namespace lulesh

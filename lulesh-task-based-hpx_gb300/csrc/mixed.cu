@@ -3,16 +3,16 @@
 // State stays double: positions, velocities, e, p, q, v and its cutoffs, the
 // element volume, the EOS with its repeat loop, the sound speed and the dt
 // minima. The element force, kinematic and Q-gradient temporaries run in
-// float, which on GB300 issues at 62x the FP64 rate.
+// float, which on GB300 issues at 60x the FP64 rate.
 //
-// Float inputs without cancellation. Every element kernel works on node
+// Float inputs without cancellation. Every element function works on node
 // coordinates and velocities relative to the element's corner 0: the stress
 // and hourglass forces, face areas, Q gradients and velocity gradient are
 // all invariant under a common shift of the corners (the hourglass vectors'
 // corner sums vanish), and relative values keep float's 24 bits for the
 // element-scale differences instead of spending them on the absolute
 // position. To form those differences with float arithmetic only, the node
-// kernel also stores each position and velocity component as a float pair
+// update also stores each position and velocity component as a float pair
 // (hi = fl(x), lo = fl(x - hi)); (hi_k - hi_0) + (lo_k - lo_0) is then within
 // about one float ulp of x_k - x_0.
 //
@@ -39,11 +39,7 @@ __device__ __forceinline__ float2 split(double v) {
     return make_float2(hi, __double2float_rn(v - double(hi)));
 }
 
-// Refreshes the float-pair mirrors of positions and velocities from the
-// double state (after the host uploads positions or velocities).
-__global__ void __launch_bounds__(kNodeBlock) k_mirror(Mesh m) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= m.numNode) return;
+__device__ __forceinline__ void mirror_node(const Mesh& m, int n) {
     m.pxp[n] = split(m.x[n]);
     m.pyp[n] = split(m.y[n]);
     m.pzp[n] = split(m.z[n]);
@@ -52,11 +48,9 @@ __global__ void __launch_bounds__(kNodeBlock) k_mirror(Mesh m) {
     m.vzp[n] = split(m.zd[n]);
 }
 
-// Stress + hourglass corner forces in float, stored combined (corner-major).
-__global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m) {
-    if (m.dtime && !m.dtime->active) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.numElem) return;
+// Stress + hourglass corner forces of element i in float, stored combined
+// (corner-major).
+__device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     const size_t N = (size_t)m.numElem;
     int nl[8];
     load_nodelist(m.nodelist, i, nl);
@@ -120,13 +114,7 @@ struct Neumaier {
     __device__ __forceinline__ double value() const { return double(s) + double(c); }
 };
 
-__global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
-    if (m.dtime) {
-        if (!m.dtime->active) return;
-        dt = m.dtime->deltatime;
-    }
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= m.numNode) return;
+__device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt) {
     const size_t N = (size_t)m.numElem;
     const int b = LD(m.nodeElemStart + n), e = LD(m.nodeElemStart + n + 1);
     Neumaier sx, sy, sz;
@@ -138,21 +126,10 @@ __global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
         sz.add(LD(m.fcz + idx));
     }
     node_update(m, n, sx.value(), sy.value(), sz.value(), dt);
-    m.pxp[n] = split(m.x[n]);
-    m.pyp[n] = split(m.y[n]);
-    m.pzp[n] = split(m.z[n]);
-    m.vxp[n] = split(m.xd[n]);
-    m.vyp[n] = split(m.yd[n]);
-    m.vzp[n] = split(m.zd[n]);
+    mirror_node(m, n);
 }
 
-__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
-    if (m.dtime) {
-        if (!m.dtime->active) return;
-        dt = m.dtime->deltatime;
-    }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.numElem) return;
+__device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt) {
     int nl[8];
     load_nodelist(m.nodelist, i, nl);
     double volume;
@@ -197,23 +174,58 @@ __global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
     update_volume(m, i, vold, relv);
 }
 
+__device__ __forceinline__ void material_elem(const Mesh& m, int t, double& dtc, double& dth) {
+    const int i = LD(m.matOrder + t);
+    const double vnew = LD(m.vnew + i), vdov = LD(m.vdov + i);
+    double ql, qq;
+    q_terms<float>(m, i, m.gvxi, m.gveta, m.gvzeta, m.gxxi, m.gxeta, m.gxzeta, vnew, vdov, ql, qq);
+    m.qq[i] = qq;
+    m.ql[i] = ql;
+    double vnewc = vnew;
+    if (m.prm.eosvmin != 0.0 && vnewc < m.prm.eosvmin) vnewc = m.prm.eosvmin;
+    if (m.prm.eosvmax != 0.0 && vnewc > m.prm.eosvmax) vnewc = m.prm.eosvmax;
+    const double ss = eos_element(m, i, vnewc, LD(m.elemRep + i));
+    dt_constraints(m.prm, ss, vdov, LD(m.arealg + i), dtc, dth);
+}
+
+// --- single-problem kernels -------------------------------------------------
+
+// Refreshes the float-pair mirrors from the double state (after the host
+// uploads positions or velocities).
+__global__ void __launch_bounds__(kNodeBlock) k_mirror(Mesh m) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < m.numNode) mirror_node(m, n);
+}
+
+__global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m) {
+    if (m.dtime && !m.dtime->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.numElem) forces_elem(m, i);
+}
+
+__global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
+    if (m.dtime) {
+        if (!m.dtime->active) return;
+        dt = m.dtime->deltatime;
+    }
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < m.numNode) nodes_node(m, n, dt);
+}
+
+__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
+    if (m.dtime) {
+        if (!m.dtime->active) return;
+        dt = m.dtime->deltatime;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.numElem) kinematics_elem(m, i, dt);
+}
+
 __global__ void __launch_bounds__(kMatBlock) k_material(Mesh m) {
     if (m.dtime && !m.dtime->active) return;
     double dtc = 1.0e+20, dth = 1.0e+20;
-    const int N = m.numElem;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
-        const int i = LD(m.matOrder + t);
-        const double vnew = LD(m.vnew + i), vdov = LD(m.vdov + i);
-        double ql, qq;
-        q_terms<float>(m, i, m.gvxi, m.gveta, m.gvzeta, m.gxxi, m.gxeta, m.gxzeta, vnew, vdov, ql, qq);
-        m.qq[i] = qq;
-        m.ql[i] = ql;
-        double vnewc = vnew;
-        if (m.prm.eosvmin != 0.0 && vnewc < m.prm.eosvmin) vnewc = m.prm.eosvmin;
-        if (m.prm.eosvmax != 0.0 && vnewc > m.prm.eosvmax) vnewc = m.prm.eosvmax;
-        const double ss = eos_element(m, i, vnewc, LD(m.elemRep + i));
-        dt_constraints(m.prm, ss, vdov, LD(m.arealg + i), dtc, dth);
-    }
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.numElem; t += gridDim.x * blockDim.x)
+        material_elem(m, t, dtc, dth);
     finish_dt_reduction(m, dtc, dth);
 }
 
@@ -240,3 +252,5 @@ int launch_material(const Mesh& m, cudaStream_t s) {
 
 }  // namespace mixed
 }  // namespace lulesh
+
+#include "batch_kernels.cuh"

@@ -156,3 +156,17 @@ def test_symmetry_matches_oracle(lulesh, oracle_mod):
     d.e[:] = vals
     o.field("e")[:] = vals
     assert d.symmetry() == o.symmetry()
+
+
+def test_batch_footprint_and_loud_failure_without_gpu(lulesh):
+    f = [lulesh.Batch.footprint(p, s) for p in ("fp64", "mixed") for s in (16, 64, 150)]
+    assert f[0] < f[1] < f[2] and f[3] < f[4] < f[5]
+    assert f[5] < f[2]  # float temporaries take less memory
+    assert f[2] / 150 ** 3 < 800  # bytes per element of the double path
+    with pytest.raises(lulesh.LuleshError) as ei:
+        lulesh.Batch.footprint("fp64", 0)
+    assert ei.value.status == lulesh.EINVAL
+    if not gpu_available():
+        with pytest.raises(lulesh.LuleshError) as ei:
+            lulesh.Batch("fp64", 1 << 20, 4)
+        assert ei.value.status == lulesh.ENODEV
