@@ -207,6 +207,13 @@ int lulesh_batch_footprint(int32_t precision, int32_t s, uint64_t* bytes);
 /* Builds the problem (Domain::Domain on the host), copies it into the pool
  * and makes it active. LULESH_ENOMEM when the pool or the slots are full. */
 int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot);
+/* Admits an existing host Domain (a view as for lulesh_dev_create, with
+ * view->time set): its whole state is copied into the pool. stoptime > 0 and
+ * max_cycles > 0 override the view's stoptime and the unlimited cycle count. */
+int lulesh_batch_admit_view(lulesh_batch* b, const lulesh_domain_view* v, double stoptime,
+                            int32_t max_cycles, int32_t* slot);
+/* Origin energy e(0) of a slot (the reference's reported result). */
+int lulesh_batch_origin_energy(lulesh_batch* b, int32_t slot, double* e0);
 /* Frees a slot (finished or not) and its pool memory. */
 int lulesh_batch_retire(lulesh_batch* b, int32_t slot);
 /* Replays the cycle graph `cycles` times, then refreshes the slot status.
@@ -224,6 +231,41 @@ int lulesh_batch_get_tuning(const lulesh_batch* b, lulesh_batch_tuning* out);
 int lulesh_batch_set_tuning(lulesh_batch* b, const lulesh_batch_tuning* t);
 /* Kernel launches issued so far (graph replays count every kernel node). */
 int64_t lulesh_batch_launch_count(const lulesh_batch* b);
+
+/* ---------------- serving loop ---------------------------------------------------------
+ * No counterpart in the reference. Serves a stream of requests with
+ * continuous batching: a worker thread builds each request's Domain on the
+ * host once it has arrived (arrival_s after the call starts, wall clock),
+ * the loop admits built requests into the resident batch whenever a slot and
+ * enough of the hbm_budget pool are free (in arrival order, later requests
+ * may pass one that does not fit yet), replays cycles of all resident
+ * problems in chunks of about sync_ms of device time, and retires each
+ * problem when it reaches its stoptime or cycle limit. Results and
+ * time-to-solution (finish - arrival) per request, p50/p99 and aggregate
+ * zone-cycles/s in stats. */
+typedef struct lulesh_request {
+    lulesh_problem problem;
+    double arrival_s;
+} lulesh_request;
+
+typedef struct lulesh_request_result {
+    int32_t cycles, err, s, pad_;
+    double arrival_s, admitted_s, finished_s, time_to_solution_s;
+    double e0; /* final origin energy */
+    int64_t zone_cycles;
+} lulesh_request_result;
+
+typedef struct lulesh_serve_stats {
+    double wall_s;             /* start to the last finish */
+    double device_s;           /* device time of the cycle replays */
+    double zone_cycles_per_s;  /* all requests' zone-cycles / wall_s */
+    double p50_s, p99_s, mean_s; /* time to solution */
+    int64_t zone_cycles, launches;
+    int32_t served, max_resident;
+} lulesh_serve_stats;
+
+int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_slots, const lulesh_request* reqs,
+                 int32_t n, double sync_ms, lulesh_request_result* results, lulesh_serve_stats* stats);
 
 /* Test hooks (no counterpart in the reference; they expose the step's
  * intermediate arrays so each kernel can be checked on its own). */

@@ -83,6 +83,23 @@ class BatchTuning(C.Structure):
                 ("pad_", C.c_int32), ("ms_per_cycle", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("problem", Problem), ("arrival_s", C.c_double)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("cycles", "err", "s", "pad_")] + \
+               [(n, C.c_double) for n in ("arrival_s", "admitted_s", "finished_s", "time_to_solution_s",
+                                          "e0")] + [("zone_cycles", C.c_int64)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("wall_s", "device_s", "zone_cycles_per_s", "p50_s", "p99_s",
+                                          "mean_s")] + \
+               [("zone_cycles", C.c_int64), ("launches", C.c_int64), ("served", C.c_int32),
+                ("max_resident", C.c_int32)]
+
+
 class DomainView(C.Structure):
     _fields_ = (
         [(n, C.c_int32) for n in ("numElem", "numNode", "sizeX", "numReg", "cost", "numSymmX",
@@ -145,6 +162,10 @@ def library() -> C.CDLL:
         "lulesh_batch_get_tuning": (i32, [vp, C.POINTER(BatchTuning)]),
         "lulesh_batch_set_tuning": (i32, [vp, C.POINTER(BatchTuning)]),
         "lulesh_batch_launch_count": (i64, [vp]),
+        "lulesh_batch_admit_view": (i32, [vp, C.POINTER(DomainView), dbl, i32, C.POINTER(i32)]),
+        "lulesh_batch_origin_energy": (i32, [vp, i32, C.POINTER(dbl)]),
+        "lulesh_serve": (i32, [i32, C.c_uint64, i32, C.POINTER(Request), i32, dbl,
+                               C.POINTER(RequestResult), C.POINTER(ServeStats)]),
         "lulesh_cbrt_portable": (dbl, [dbl]),
         "lulesh_strerror": (C.c_char_p, [i32]),
     }
@@ -329,6 +350,27 @@ def pipe_rates() -> dict:
     out = (C.c_double * 5)()
     _check(library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
     return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma"), list(out)))
+
+
+def serve(requests: list[dict], precision: str = "mixed", hbm_budget: int = 160 << 30,
+          max_slots: int = 256, sync_ms: float = 20.0) -> tuple[list[dict], dict]:
+    """Continuous-batching serving loop (lulesh_serve). Each request is a dict
+    with s, nr, balance, cost, energy_scale, stoptime, max_cycles (as
+    Batch.admit) and arrival_s (seconds after the call starts)."""
+    n = len(requests)
+    arr = (Request * n)()
+    for i, r in enumerate(requests):
+        arr[i].problem = Problem(r["s"], r.get("nr", 11), r.get("balance", 1), r.get("cost", 1),
+                                 r.get("energy_scale", 1.0), r.get("stoptime", 0.0),
+                                 r.get("max_cycles", 0), 0)
+        arr[i].arrival_s = r["arrival_s"]
+    res = (RequestResult * n)()
+    st = ServeStats()
+    _check(library().lulesh_serve(PRECISION[precision], hbm_budget, max_slots, arr, n, sync_ms, res,
+                                  C.byref(st)), "lulesh_serve")
+    out = [{k: getattr(x, k) for k, _ in RequestResult._fields_ if k != "pad_"} for x in res]
+    stats = {k: getattr(st, k) for k, _ in ServeStats._fields_}
+    return out, stats
 
 
 def _tuning_dict(t: BatchTuning) -> dict:

@@ -42,6 +42,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("probe.cu", []),
     ("batch.cu", []),
+    ("serve.cu", []),
     ("domain.cpp", ["-x", "cu", "--fmad=false"]),
 ]
 
@@ -85,7 +86,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                 print(" ".join(cmd), file=sys.stderr)
         list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB, objs):
-        _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"])
+        _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lpthread"])
     drv = CSRC / "driver.cpp"
     if drv.exists() and (force or _stale(EXE, [drv, LIB] + headers)):
         _run([cc, *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-ffp-contract=off", f"-I{ROOT / 'include'}",

@@ -381,6 +381,24 @@ int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot_o
     if (!b || !p) return LULESH_EINVAL;
     if (p->s < 1 || p->s > 640 || p->nr < 1 || p->balance < 0 || p->cost < 0 || !(p->energy_scale > 0.0))
         return LULESH_EINVAL;
+    // refuse before the host set-up when the problem cannot fit
+    bool free_slot = false;
+    for (const Slot& sl : b->slots) free_slot |= !sl.in_use;
+    const int ne = p->s * p->s * p->s, nn = (p->s + 1) * (p->s + 1) * (p->s + 1);
+    if (!free_slot || b->pool.largest_free() < lulesh::mesh_bytes(b->precision, ne, nn)) return LULESH_ENOMEM;
+    lulesh_domain* hd = nullptr;
+    int st = lulesh_domain_create(p->s, p->nr, p->balance, p->cost, p->energy_scale, &hd);
+    if (st == LULESH_OK)
+        st = lulesh_batch_admit_view(b, lulesh_domain_get_view(hd), p->stoptime, p->max_cycles, slot_out);
+    lulesh_domain_destroy(hd);
+    return st;
+}
+
+int lulesh_batch_admit_view(lulesh_batch* b, const lulesh_domain_view* v, double stoptime,
+                            int32_t max_cycles, int32_t* slot_out) {
+    if (!b || !v || !v->time) return LULESH_EINVAL;
+    int st = lulesh::validate_view(v);
+    if (st != LULESH_OK) return st;
     int slot = -1;
     for (int i = 0; i < int(b->slots.size()); ++i)
         if (!b->slots[i].in_use) {
@@ -388,21 +406,16 @@ int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot_o
             break;
         }
     if (slot < 0) return LULESH_ENOMEM;
-    const int ne = p->s * p->s * p->s, nn = (p->s + 1) * (p->s + 1) * (p->s + 1);
+    const int ne = v->numElem, nn = v->numNode;
     const size_t bytes = lulesh::mesh_bytes(b->precision, ne, nn);
     const size_t off = b->pool.alloc(bytes);
     if (off == SIZE_MAX) return LULESH_ENOMEM;
-    lulesh_domain* hd = nullptr;
-    int st = lulesh_domain_create(p->s, p->nr, p->balance, p->cost, p->energy_scale, &hd);
-    if (st == LULESH_OK) st = lulesh::validate_view(lulesh_domain_get_view(hd));
     Mesh m{};
-    if (st == LULESH_OK) st = lulesh::mesh_init(m, b->pool_base + off, lulesh_domain_get_view(hd), b->precision, b->stream);
+    st = lulesh::mesh_init(m, b->pool_base + off, v, b->precision, b->stream);
     if (st != LULESH_OK) {
-        lulesh_domain_destroy(hd);
         b->pool.release(off, bytes);
         return st;
     }
-    const lulesh_domain_view* v = lulesh_domain_get_view(hd);
     m.result = b->d_results + slot;
     m.dtime = b->d_times + slot;
     m.partials = nullptr;
@@ -417,9 +430,9 @@ int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot_o
     t.deltatimemultlb = ts->deltatimemultlb;
     t.deltatimemultub = ts->deltatimemultub;
     t.dtmax = ts->dtmax;
-    t.stoptime = p->stoptime > 0.0 ? p->stoptime : ts->stoptime;
-    t.cycle = 0;
-    t.max_cycles = p->max_cycles > 0 ? p->max_cycles : INT32_MAX;
+    t.stoptime = stoptime > 0.0 ? stoptime : ts->stoptime;
+    t.cycle = ts->cycle;
+    t.max_cycles = max_cycles > 0 ? max_cycles : INT32_MAX;
     t.active = 1;
     StepResult r{};
     r.dtcourant = r.dthydro = 1.0e+20;
@@ -433,7 +446,6 @@ int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot_o
         sl.repValue.push_back(kv.first);
         sl.repCount.push_back(kv.second);
     }
-    lulesh_domain_destroy(hd);
     b->h_meshes[slot] = m;
     b->h_times[slot] = t;
     b->h_results[slot] = r;
@@ -444,11 +456,18 @@ int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot_o
     sl.in_use = true;
     sl.off = off;
     sl.bytes = bytes;
-    sl.s = p->s;
+    sl.s = v->sizeX;
     sl.numElem = ne;
     sl.numNode = nn;
     b->tiles_dirty = true;
     if (slot_out) *slot_out = slot;
+    return LULESH_OK;
+}
+
+int lulesh_batch_origin_energy(lulesh_batch* b, int32_t slot, double* e0) {
+    if (!b || !e0 || slot < 0 || slot >= int(b->slots.size()) || !b->slots[slot].in_use) return LULESH_EINVAL;
+    BCK(cudaMemcpyAsync(e0, b->h_meshes[slot].e, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
     return LULESH_OK;
 }
 
