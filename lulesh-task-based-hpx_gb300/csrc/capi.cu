@@ -116,6 +116,8 @@ int check_view(const lulesh_domain_view* v) {
         if (v->nodeElemCornerList[k] < 0 || v->nodeElemCornerList[k] >= 8 * ne) return LULESH_EINVAL;
     for (int i = 0; i < ne; ++i)
         if (v->regNumList[i] < 1 || v->regNumList[i] > v->numReg) return LULESH_EINVAL;
+    for (int n = 0; n < nn; ++n)
+        if (!(v->nodalMass[n] > 0.0)) return LULESH_EINVAL;  // a = f / m needs m > 0
     const int32_t* sy[] = {v->symmX, v->symmY, v->symmZ};
     const int32_t cnt[] = {v->numSymmX, v->numSymmY, v->numSymmZ};
     for (int a = 0; a < 3; ++a) {
@@ -133,6 +135,7 @@ void carve_mesh(Mesh& m, Arena& a, bool mixed, int ne, int nn) {
                        &m.fz})
         *f = a.take<double>(nn);
     m.nodalMass = a.take<double>(nn);
+    m.invMass = a.take<double>(nn);
     m.nodeSymm = a.take<uint8_t>(nn);
     m.nodelist = a.take<int32_t>(8 * size_t(ne));
     for (const int32_t** f : {&m.lxim, &m.lxip, &m.letam, &m.letap, &m.lzetam, &m.lzetap, &m.elemBC})
@@ -207,6 +210,8 @@ int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaS
     for (int k = 0; k < v->numSymmX; ++k) symm[v->symmX[k]] |= 1;
     for (int k = 0; k < v->numSymmY; ++k) symm[v->symmY[k]] |= 2;
     for (int k = 0; k < v->numSymmZ; ++k) symm[v->symmZ[k]] |= 4;
+    std::vector<double> invMass(nn);
+    for (int k = 0; k < nn; ++k) invMass[k] = 1.0 / v->nodalMass[k];
     std::vector<int32_t> rep(ne), order(ne);
     for (int i = 0; i < ne; ++i) rep[i] = region_rep(v->regNumList[i] - 1, v->numReg, v->cost);
     for (int i = 0; i < ne; ++i) order[i] = i;
@@ -215,6 +220,7 @@ int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaS
     const size_t eb = sizeof(int32_t) * size_t(ne);
     const Copy consts[] = {
         {const_cast<double*>(m.nodalMass), v->nodalMass, sizeof(double) * size_t(nn)},
+        {const_cast<double*>(m.invMass), invMass.data(), sizeof(double) * size_t(nn)},
         {const_cast<uint8_t*>(m.nodeSymm), symm.data(), size_t(nn)},
         {const_cast<int32_t*>(m.nodelist), v->nodelist, 8 * eb},
         {const_cast<int32_t*>(m.lxim), v->lxim, eb},

@@ -49,12 +49,13 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
         const double sig = -LD(m.p + i) - LD(m.q + i);
         if (jac_det(jacobian(x, y, z)) == 0) raise_error(m.result, i, PHASE_FORCES);
         double nx[8], ny[8], nz[8];
-        node_normals(nx, ny, nz, x, y, z);
+        node_normals(nx, ny, nz, x, y, z);   // 16 x the normals
+        const double sig16 = sig * 0.0625;  // exact: a power of two
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            m.fsx[k * N + i] = -(sig * nx[k]);
-            m.fsy[k * N + i] = -(sig * ny[k]);
-            m.fsz[k * N + i] = -(sig * nz[k]);
+            m.fsx[k * N + i] = -(sig16 * nx[k]);
+            m.fsy[k * N + i] = -(sig16 * ny[k]);
+            m.fsz[k * N + i] = -(sig16 * nz[k]);
         }
     }
 
@@ -68,10 +69,10 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     {
         double dvdx[8], dvdy[8], dvdz[8];
         volume_derivs(dvdx, dvdy, dvdz, x, y, z);
-        hourgam_all(hg, x, y, z, dvdx, dvdy, dvdz, 1.0 / determ);
+        hourgam_all(hg, x, y, z, dvdx, dvdy, dvdz, rcp(determ));
     }
     const double coefficient =
-        -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) / cube_root(determ);
+        quot(-m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i), cube_root(determ));
     double vel[8], f[8];
     gather8(m.xd, nl, vel);
     fb_force_axis(hg, vel, coefficient, f);
@@ -117,11 +118,11 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     gather8(m.y, nl, y);
     gather8(m.z, nl, z);
     const double volume = hex_volume(x, y, z);
-    const double relv = volume / LD(m.volo + i);
+    const double relv = quot(volume, LD(m.volo + i));
     const double vold = m.v[i];
     m.vnew[i] = relv;
     m.delv[i] = relv - vold;
-    m.arealg[i] = 4.0 * volume / sqrt(max_face_area(x, y, z));
+    m.arealg[i] = div_sqrt(4.0 * volume, max_face_area(x, y, z));
 
     gather8(m.xd, nl, xv);
     gather8(m.yd, nl, yv);

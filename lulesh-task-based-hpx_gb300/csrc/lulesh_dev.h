@@ -67,6 +67,7 @@ struct Mesh {
     // node-centred
     double *x, *y, *z, *xd, *yd, *zd, *xdd, *ydd, *zdd, *fx, *fy, *fz;
     const double* nodalMass;
+    const double* invMass;  // 1 / nodalMass (fast variants multiply by it)
     const uint8_t* nodeSymm;
     // element-centred
     const int32_t* nodelist;

@@ -61,7 +61,8 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
 
     float fx[8], fy[8], fz[8];
     {
-        const float sig = float(-LD(m.p + i) - LD(m.q + i));
+        // node_normals returns 16 x the normals: fold the 1/16 into the stress
+        const float sig = float(-LD(m.p + i) - LD(m.q + i)) * 0.0625f;
         if (jac_det(jacobian(x, y, z)) == 0.0f) raise_error(m.result, i, PHASE_FORCES);
         float nx[8], ny[8], nz[8];
         node_normals(nx, ny, nz, x, y, z);
@@ -140,7 +141,7 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
         gather8(m.z, nl, zd8);
         volume = hex_volume(xd8, yd8, zd8);  // double: relative volume and delv need it
     }
-    const double relv = volume / LD(m.volo + i);
+    const double relv = quot(volume, LD(m.volo + i));
     const double vold = m.v[i];
     m.vnew[i] = relv;
     m.delv[i] = relv - vold;
@@ -149,7 +150,7 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     rel8(m.pxp, nl, x);
     rel8(m.pyp, nl, y);
     rel8(m.pzp, nl, z);
-    m.arealg[i] = double(4.0f * float(volume) / sqrtf(max_face_area(x, y, z)));
+    m.arealg[i] = double(div_sqrt(4.0f * float(volume), max_face_area(x, y, z)));
     rel8(m.vxp, nl, xv);
     rel8(m.vyp, nl, yv);
     rel8(m.vzp, nl, zv);

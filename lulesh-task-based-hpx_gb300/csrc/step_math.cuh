@@ -133,26 +133,82 @@ __device__ __forceinline__ R shape_derivs(const Jac<R>& j, R b[3][4]) {
     return R(8.) * (j.fjxet * cjxet + j.fjyet * cjyet + j.fjzet * cjzet);
 }
 
+// Division helpers. x / refdens is x itself when refdens is 1 (the
+// reference's value), so that case skips the divide and stays bit-exact.
+// a / sqrt(b) uses the reciprocal square root in the fast variants (one
+// rounding more, a few FP64-pipe slots fewer) and the reference's divide and
+// square root in the exact one.
+template <bool UNIT_RHO>
+__device__ __forceinline__ double over_rho(double x, const lulesh_params& P) {
+    return UNIT_RHO ? x : x / P.refdens;
+}
+
+// Reciprocal and quotient. Exact variant: IEEE 1/x and a/b. Fast variants:
+// Newton-Raphson on the hardware's approximate double reciprocal
+// (rcp.approx.ftz.f64, which issues on the multi-function unit, not the
+// FP64 pipe): two steps y <- y + y (1 - x y) take its ~2^-22 start to full
+// double precision, within about 1 ulp of 1/x for finite, nonzero, normal x
+// (every divisor of the step is such a number). a/b becomes a * (1/b), one
+// rounding more. This saves FP64-pipe slots over the IEEE divide.
+__device__ __forceinline__ double rcp(double x) {
+#if LULESH_EXACT
+    return 1.0 / x;
+#else
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+#endif
+}
+__device__ __forceinline__ float rcp(float x) { return 1.0f / x; }
+
+template <class R>
+__device__ __forceinline__ R quot(R a, R b) {
+#if LULESH_EXACT
+    return a / b;
+#else
+    return a * rcp(b);
+#endif
+}
+
+__device__ __forceinline__ double recip_sqrt(double b) { return rsqrt(b); }
+__device__ __forceinline__ float recip_sqrt(float b) { return rsqrtf(b); }
+
+template <class R>
+__device__ __forceinline__ R div_sqrt(R a, R b) {
+#if LULESH_EXACT
+    return a / sqrt(b);
+#else
+    return a * recip_sqrt(b);
+#endif
+}
+
 // One face's area vector added to its four corners (SumElemFaceNormal,
 // lulesh.cc:378-409); A..D are the face corners in the reference's order.
+// The reference's factors 0.5 (bisectors) and 0.25 (area) are left out: the
+// normals come out scaled by exactly 16, and callers scale the stress by
+// 1/16 instead. Powers of two commute with rounding, so this is bit-exact.
 template <int A, int B, int C, int D, class R>
 __device__ __forceinline__ void face_normal(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
                                             const R z[8]) {
-    const R bisX0 = R(0.5) * (x[D] + x[C] - x[B] - x[A]);
-    const R bisY0 = R(0.5) * (y[D] + y[C] - y[B] - y[A]);
-    const R bisZ0 = R(0.5) * (z[D] + z[C] - z[B] - z[A]);
-    const R bisX1 = R(0.5) * (x[C] + x[B] - x[D] - x[A]);
-    const R bisY1 = R(0.5) * (y[C] + y[B] - y[D] - y[A]);
-    const R bisZ1 = R(0.5) * (z[C] + z[B] - z[D] - z[A]);
-    const R ax = R(0.25) * (bisY0 * bisZ1 - bisZ0 * bisY1);
-    const R ay = R(0.25) * (bisZ0 * bisX1 - bisX0 * bisZ1);
-    const R az = R(0.25) * (bisX0 * bisY1 - bisY0 * bisX1);
+    const R bisX0 = (x[D] + x[C] - x[B] - x[A]);
+    const R bisY0 = (y[D] + y[C] - y[B] - y[A]);
+    const R bisZ0 = (z[D] + z[C] - z[B] - z[A]);
+    const R bisX1 = (x[C] + x[B] - x[D] - x[A]);
+    const R bisY1 = (y[C] + y[B] - y[D] - y[A]);
+    const R bisZ1 = (z[C] + z[B] - z[D] - z[A]);
+    const R ax = (bisY0 * bisZ1 - bisZ0 * bisY1);
+    const R ay = (bisZ0 * bisX1 - bisX0 * bisZ1);
+    const R az = (bisX0 * bisY1 - bisY0 * bisX1);
     nx[A] += ax; nx[B] += ax; nx[C] += ax; nx[D] += ax;
     ny[A] += ay; ny[B] += ay; ny[C] += ay; ny[D] += ay;
     nz[A] += az; nz[B] += az; nz[C] += az; nz[D] += az;
 }
 
-// CalcElemNodeNormals (lulesh.cc:413-451), faces in the reference's order.
+// CalcElemNodeNormals (lulesh.cc:413-451), faces in the reference's order;
+// the result is 16 times the reference's normals (see face_normal).
 template <class R>
 __device__ __forceinline__ void node_normals(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
                                              const R z[8]) {
@@ -180,9 +236,17 @@ __device__ __forceinline__ void volu_der(R dvdx[8], R dvdy[8], R dvdz[8], const 
                  (x3 + x4) * (z0 + z4) + (x2 + x5) * (z3 + z5) - (x3 + x5) * (z2 + z5);
     const R dz = -(y1 + y2) * (x0 + x1) + (y0 + y1) * (x1 + x2) - (y0 + y4) * (x3 + x4) +
                  (y3 + y4) * (x0 + x4) + (y2 + y5) * (x3 + x5) - (y3 + y5) * (x2 + x5);
+#if LULESH_EXACT
     dvdx[K] = dx * twelfth;
     dvdy[K] = dy * twelfth;
     dvdz[K] = dz * twelfth;
+#else
+    // fast variants: 12 x the derivative; hourgam_all folds 1/12 into volinv
+    (void)twelfth;
+    dvdx[K] = dx;
+    dvdy[K] = dy;
+    dvdz[K] = dz;
+#endif
 }
 
 // CalcElemVolumeDerivative (lulesh.cc:495-523).
@@ -228,10 +292,15 @@ __device__ __forceinline__ void hourgam_mode(R hg[8][4], const R x[8], const R y
         hg[k][M] = R(gamma_sign(M, k)) - volinv * (dvdx[k] * hx + dvdy[k] * hy + dvdz[k] * hz);
 }
 
+// volinv = 1 / (volo v); in the fast variants the volume derivatives come
+// 12 times too large (volu_der) and the 1/12 is applied here, once.
 template <class R>
 __device__ __forceinline__ void hourgam_all(R hg[8][4], const R x[8], const R y[8], const R z[8],
                                             const R dvdx[8], const R dvdy[8], const R dvdz[8],
                                             R volinv) {
+#if !LULESH_EXACT
+    volinv = volinv * (R(1.0) / R(12.0));
+#endif
     hourgam_mode<0>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
     hourgam_mode<1>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
     hourgam_mode<2>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
@@ -247,9 +316,18 @@ __device__ __forceinline__ void fb_force_axis(const R hg[8][4], const R vel[8], 
     for (int m = 0; m < 4; ++m)
         h[m] = hg[0][m] * vel[0] + hg[1][m] * vel[1] + hg[2][m] * vel[2] + hg[3][m] * vel[3] +
                hg[4][m] * vel[4] + hg[5][m] * vel[5] + hg[6][m] * vel[6] + hg[7][m] * vel[7];
+#if LULESH_EXACT
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         out[k] = coefficient * (hg[k][0] * h[0] + hg[k][1] * h[1] + hg[k][2] * h[2] + hg[k][3] * h[3]);
+#else
+    // fast variants: the coefficient scales the 4 mode amplitudes, not the 8 corners
+#pragma unroll
+    for (int m = 0; m < 4; ++m) h[m] *= coefficient;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        out[k] = hg[k][0] * h[0] + hg[k][1] * h[1] + hg[k][2] * h[2] + hg[k][3] * h[3];
+#endif
 }
 
 // AreaFace (lulesh.cc:678-692) of the face with corners A..D.
@@ -292,7 +370,7 @@ __device__ __forceinline__ void q_gradients(const R x[8], const R y[8], const R 
                                             const R yv[8], const R zv[8], R vol, R g[6]) {
     const R ptiny = R(1.e-36);
     const R q = R(0.25), mq = R(-0.25);
-    const R norm = R(1.0) / (vol + ptiny);
+    const R norm = rcp(vol + ptiny);
     const R dxj = mq * ((x[0] + x[1] + x[5] + x[4]) - (x[3] + x[2] + x[6] + x[7]));
     const R dyj = mq * ((y[0] + y[1] + y[5] + y[4]) - (y[3] + y[2] + y[6] + y[7]));
     const R dzj = mq * ((z[0] + z[1] + z[5] + z[4]) - (z[3] + z[2] + z[6] + z[7]));
@@ -308,7 +386,7 @@ __device__ __forceinline__ void q_gradients(const R x[8], const R y[8], const R 
     ax = dyi * dzj - dzi * dyj;
     ay = dzi * dxj - dxi * dzj;
     az = dxi * dyj - dyi * dxj;
-    g[5] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
+    g[5] = div_sqrt(vol, ax * ax + ay * ay + az * az + ptiny);
     ax *= norm;
     ay *= norm;
     az *= norm;
@@ -321,7 +399,7 @@ __device__ __forceinline__ void q_gradients(const R x[8], const R y[8], const R 
     ax = dyj * dzk - dzj * dyk;
     ay = dzj * dxk - dxj * dzk;
     az = dxj * dyk - dyj * dxk;
-    g[3] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
+    g[3] = div_sqrt(vol, ax * ax + ay * ay + az * az + ptiny);
     ax *= norm;
     ay *= norm;
     az *= norm;
@@ -334,7 +412,7 @@ __device__ __forceinline__ void q_gradients(const R x[8], const R y[8], const R 
     ax = dyk * dzi - dzk * dyi;
     ay = dzk * dxi - dxk * dzi;
     az = dxk * dyi - dyk * dxi;
-    g[4] = vol / sqrt(ax * ax + ay * ay + az * az + ptiny);
+    g[4] = div_sqrt(vol, ax * ax + ay * ay + az * az + ptiny);
     ax *= norm;
     ay *= norm;
     az *= norm;
@@ -352,7 +430,7 @@ __device__ __forceinline__ R vel_grad_trace(const R xh[8], const R yh[8], const 
                                             const R xv[8], const R yv[8], const R zv[8]) {
     R b[3][4];
     const R detJ = shape_derivs(jacobian(xh, yh, zh), b);
-    const R inv = R(1.0) / detJ;
+    const R inv = rcp(detJ);
     const R dxx = inv * (b[0][0] * (xv[0] - xv[6]) + b[0][1] * (xv[1] - xv[7]) +
                          b[0][2] * (xv[2] - xv[4]) + b[0][3] * (xv[3] - xv[5]));
     const R dyy = inv * (b[1][0] * (yv[0] - yv[6]) + b[1][1] * (yv[1] - yv[7]) +
@@ -373,7 +451,7 @@ __device__ __forceinline__ R limiter(const R* __restrict__ dv, int i, int bm, in
                                      R max_slope) {
     const R ptiny = R(1.e-36);
     const R self = LD(dv + i);
-    const R norm = R(1.) / (self + ptiny);
+    const R norm = rcp(self + ptiny);
     R delvm, delvp;
     if (bm == comm_m || bm == 0) delvm = LD(dv + nm);
     else if (bm == symm_m) delvm = self;
@@ -421,7 +499,7 @@ __device__ __forceinline__ void q_terms(const Mesh& m, int i, const R* dvxi, con
     if (dxi > R(0.)) dxi = R(0.);
     if (deta > R(0.)) deta = R(0.);
     if (dzeta > R(0.)) dzeta = R(0.);
-    const R rho = R(LD(m.elemMass + i) / (LD(m.volo + i) * vnew));
+    const R rho = R(quot(LD(m.elemMass + i), LD(m.volo + i) * vnew));
     const R qlin = -R(P.qlc_monoq) * rho *
                    (dxi * (R(1.) - phixi) + deta * (R(1.) - phieta) + dzeta * (R(1.) - phizeta));
     const R qquad = R(P.qqc_monoq) * rho *
@@ -444,46 +522,62 @@ __device__ __forceinline__ double eos_pressure(double& bvc, double& pbvc, double
 }
 
 __device__ __forceinline__ double ss_guard(double ssc) {
+#if LULESH_EXACT
     return (ssc <= .1111111e-36) ? .3333333e-18 : sqrt(ssc);
+#else
+    return (ssc <= .1111111e-36) ? .3333333e-18 : ssc * rsqrt(ssc);  // sqrt, one rounding more
+#endif
 }
+
+// The reference's "+ 0.5 * work" terms add 0.5 * 0 (work is zero,
+// lulesh.cc:1749); adding +0 only turns a -0 into +0, so the fast variants
+// leave them out.
+#if LULESH_EXACT
+#define LULESH_PLUS_ZERO_WORK +0.5 * 0.0
+#else
+#define LULESH_PLUS_ZERO_WORK
+#endif
 
 // rep evaluations of EvalEOSAllInOneTask (lulesh.cc:1692-1871) for element i,
 // each from the saved state, then the sound speed and the save of
 // CalcSoundSpeedForElemsAndSaveTask (lulesh.cc:1873-1904). Returns ss.
-__device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc, int rep) {
+// UNIT_RHO: refdens == 1, so the divisions by it are identities.
+template <bool UNIT_RHO>
+__device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, int rep) {
     const lulesh_params& P = m.prm;
     double e_new = 0., p_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
     for (int r = 0; r < rep; ++r) {
         // Each evaluation re-reads its inputs from memory as the reference's
-        // EvalEOSInit does (lulesh.cc:1720-1727); the barrier keeps the
-        // compiler from hoisting the loop-invariant evaluation out of the
-        // repeat loop, so the repeat count stays real work.
+        // EvalEOSInit does (lulesh.cc:1720-1727), and vnewc is made opaque,
+        // so the compiler can hoist no part of the evaluation out of the
+        // repeat loop: the repeat count stays real work.
         asm volatile("" ::: "memory");
+        asm volatile("" : "+d"(vnewc));
         const double e_old = m.e[i], delvc = m.delv[i], q_old = m.q[i];
         double p_old = m.p[i];
         const double qq_old = m.qq[i], ql_old = m.ql[i];
-        double comp = 1. / vnewc - 1.;
+        double comp = rcp(vnewc) - 1.;
         const double vchalf = vnewc - delvc * .5;
-        double compHalf = 1. / vchalf - 1.;
+        double compHalf = rcp(vchalf) - 1.;
         if (P.eosvmin != 0. && vnewc <= P.eosvmin) compHalf = comp;
         if (P.eosvmax != 0.0 && vnewc >= P.eosvmax) {
             p_old = 0.;
             comp = 0.;
             compHalf = 0.;
         }
-        // predictor; the reference's "+ 0.5 * work" term adds 0.5 * 0
-        e_new = e_old - 0.5 * delvc * (p_old + q_old) + 0.5 * 0.0;
+        // predictor
+        e_new = e_old - 0.5 * delvc * (p_old + q_old) LULESH_PLUS_ZERO_WORK;
         if (e_new < P.emin) e_new = P.emin;
         const double pHalf = eos_pressure(bvc, pbvc, e_new, compHalf, vnewc, P);
-        const double vhalf = 1. / (1. + compHalf);
+        const double vhalf = rcp(1. + compHalf);
         if (delvc > 0.) {
             q_new = 0.;
         } else {
-            const double ssc = ss_guard((pbvc * e_new + vhalf * vhalf * bvc * pHalf) / P.refdens);
+            const double ssc = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vhalf * vhalf * bvc * pHalf), P));
             q_new = (ssc * ql_old + qq_old);
         }
         e_new = e_new + 0.5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (pHalf + q_new));
-        e_new = e_new + 0.5 * 0.0;
+        e_new = e_new LULESH_PLUS_ZERO_WORK;
         if (fabs(e_new) < P.e_cut) e_new = 0.0;
         if (e_new < P.emin) e_new = P.emin;
         p_new = eos_pressure(bvc, pbvc, e_new, comp, vnewc, P);
@@ -494,7 +588,7 @@ __device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc
             if (delvc > 0.) {
                 q_tilde = 0.;
             } else {
-                const double ssc = ss_guard((pbvc * e_new + vnewc * vnewc * bvc * p_new) / P.refdens);
+                const double ssc = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vnewc * vnewc * bvc * p_new), P));
                 q_tilde = (ssc * ql_old + qq_old);
             }
             e_new = e_new -
@@ -504,17 +598,21 @@ __device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc
         }
         p_new = eos_pressure(bvc, pbvc, e_new, comp, vnewc, P);
         if (delvc <= 0.) {
-            const double ssc = ss_guard((pbvc * e_new + vnewc * vnewc * bvc * p_new) / P.refdens);
+            const double ssc = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vnewc * vnewc * bvc * p_new), P));
             q_new = (ssc * ql_old + qq_old);
             if (fabs(q_new) < P.q_cut) q_new = 0.;
         }
     }
-    const double sst = ss_guard((pbvc * e_new + vnewc * vnewc * bvc * p_new) / P.refdens);
+    const double sst = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vnewc * vnewc * bvc * p_new), P));
     m.ss[i] = sst;
     m.p[i] = p_new;
     m.e[i] = e_new;
     m.q[i] = q_new;
     return sst;
+}
+
+__device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc, int rep) {
+    return m.prm.refdens == 1.0 ? eos_body<true>(m, i, vnewc, rep) : eos_body<false>(m, i, vnewc, rep);
 }
 
 // Courant and hydro constraints of one element (lulesh.cc:1938-1974),
@@ -525,10 +623,9 @@ __device__ __forceinline__ void dt_constraints(const lulesh_params& P, double ss
     const double qqc2 = 64.0 * P.qqc * P.qqc;
     double dtf = ss * ss;
     if (vdov < 0.0) dtf += qqc2 * arealg * arealg * vdov * vdov;
-    dtf = sqrt(dtf);
-    dtf = arealg / dtf;
+    dtf = div_sqrt(arealg, dtf);  // arealg / sqrt(dtf)
     dtc = fmin(dtc, dtf);
-    dth = fmin(dth, P.dvovmax / (fabs(vdov) + 1.e-20));
+    dth = fmin(dth, quot(P.dvovmax, fabs(vdov) + 1.e-20));
 }
 
 // Block-wide min of (a, b); the result is valid in thread 0.
@@ -596,8 +693,14 @@ __device__ __forceinline__ void node_update(const Mesh& m, int n, double fx, dou
     m.fx[n] = fx;
     m.fy[n] = fy;
     m.fz[n] = fz;
+#if LULESH_EXACT
     const double mass = LD(m.nodalMass + n);
     double ax = fx / mass, ay = fy / mass, az = fz / mass;
+#else
+    // fast variants: the reciprocal nodal mass is precomputed once per handle
+    const double im = LD(m.invMass + n);
+    double ax = fx * im, ay = fy * im, az = fz * im;
+#endif
     const unsigned sym = LD(m.nodeSymm + n);
     if (sym & 1u) ax = 0.0;
     if (sym & 2u) ay = 0.0;
