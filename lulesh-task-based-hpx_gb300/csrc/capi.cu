@@ -130,7 +130,8 @@ int check_view(const lulesh_domain_view* v) {
 
 // Lays out the mesh arrays of one problem in the arena; with base == null it
 // only measures.
-void carve_mesh(Mesh& m, Arena& a, bool mixed, int ne, int nn) {
+void carve_mesh(Mesh& m, Arena& a, int precision, int ne, int nn) {
+    const bool mixed = precision == LULESH_MIXED;
     for (double** f : {&m.x, &m.y, &m.z, &m.xd, &m.yd, &m.zd, &m.xdd, &m.ydd, &m.zdd, &m.fx, &m.fy,
                        &m.fz})
         *f = a.take<double>(nn);
@@ -155,8 +156,10 @@ void carve_mesh(Mesh& m, Arena& a, bool mixed, int ne, int nn) {
         for (float** f : {&m.gvxi, &m.gveta, &m.gvzeta, &m.gxxi, &m.gxeta, &m.gxzeta})
             *f = a.take<float>(ne);
     } else {
-        for (double** f : {&m.fsx, &m.fsy, &m.fsz, &m.fhx, &m.fhy, &m.fhz})
-            *f = a.take<double>(8 * size_t(ne));
+        for (double** f : {&m.fsx, &m.fsy, &m.fsz}) *f = a.take<double>(8 * size_t(ne));
+        // separate hourglass corner forces only for the exact variant
+        if (precision == LULESH_FP64_EXACT)
+            for (double** f : {&m.fhx, &m.fhy, &m.fhz}) *f = a.take<double>(8 * size_t(ne));
         for (double** f : {&m.dvxi, &m.dveta, &m.dvzeta, &m.dxxi, &m.dxeta, &m.dxzeta})
             *f = a.take<double>(ne);
     }
@@ -166,7 +169,7 @@ void carve_mesh(Mesh& m, Arena& a, bool mixed, int ne, int nn) {
 // reduction scratch and the graph form's time state.
 void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     Mesh& m = d->m;
-    carve_mesh(m, a, d->precision == LULESH_MIXED, ne, nn);
+    carve_mesh(m, a, d->precision, ne, nn);
     m.partials = a.take<lulesh::DtPartial>(matGrid);
     m.result = a.take<StepResult>(1);
     d->d_time = a.take<DevTime>(1);
@@ -510,12 +513,13 @@ int lulesh_dev_corner_forces(lulesh_dev* d, double* fx8, double* fy8, double* fz
         }
         return LULESH_OK;
     }
-    std::vector<double> s(n8), h(n8);
+    // the exact variant keeps stress and hourglass apart; the fast one stores the sum
+    std::vector<double> s(n8), h(n8, 0.0);
     const double* ss[3] = {m.fsx, m.fsy, m.fsz};
     const double* hh[3] = {m.fhx, m.fhy, m.fhz};
     for (int a = 0; a < 3; ++a) {
         CK(cudaMemcpy(s.data(), ss[a], n8 * sizeof(double), cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(h.data(), hh[a], n8 * sizeof(double), cudaMemcpyDeviceToHost));
+        if (hh[a]) CK(cudaMemcpy(h.data(), hh[a], n8 * sizeof(double), cudaMemcpyDeviceToHost));
         for (size_t i = 0; i < N; ++i)
             for (int k = 0; k < 8; ++k) outs[a][8 * i + k] = s[k * N + i] + h[k * N + i];
     }
@@ -591,14 +595,14 @@ int validate_view(const lulesh_domain_view* v) { return check_view(v); }
 size_t mesh_bytes(int precision, int numElem, int numNode) {
     Mesh m{};
     Arena a;
-    carve_mesh(m, a, precision == LULESH_MIXED, numElem, numNode);
+    carve_mesh(m, a, precision, numElem, numNode);
     return (a.used + 255) & ~size_t(255);
 }
 
 int mesh_init(Mesh& m, char* base, const lulesh_domain_view* v, int precision, cudaStream_t s) {
     Arena a;
     a.base = base;
-    carve_mesh(m, a, precision == LULESH_MIXED, v->numElem, v->numNode);
+    carve_mesh(m, a, precision, v->numElem, v->numNode);
     m.numElem = v->numElem;
     m.numNode = v->numNode;
     m.prm = v->params;

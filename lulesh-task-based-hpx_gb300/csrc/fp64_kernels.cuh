@@ -71,21 +71,37 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
         volume_derivs(dvdx, dvdy, dvdz, x, y, z);
         hourgam_all(hg, x, y, z, dvdx, dvdy, dvdz, rcp(determ));
     }
+#if LULESH_EXACT
     const double coefficient =
-        quot(-m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i), cube_root(determ));
+        -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) / cube_root(determ);
+#else
+    // times the reciprocal cube root: one library call instead of cbrt + divide
+    const double coefficient = -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) * rcbrt(determ);
+#endif
     double vel[8], f[8];
-    gather8(m.xd, nl, vel);
-    fb_force_axis(hg, vel, coefficient, f);
+#if LULESH_EXACT
+    // separate hourglass arrays: the gather adds stress then hourglass
+    double* outs[3] = {m.fhx, m.fhy, m.fhz};
+#else
+    // fast variant: one corner force per corner, stress + hourglass; the
+    // stress values written above are re-read from L2 and overwritten, so
+    // HBM sees a single 24-double store per element
+    double* outs[3] = {m.fsx, m.fsy, m.fsz};
+#endif
+    const double* vels[3] = {m.xd, m.yd, m.zd};
 #pragma unroll
-    for (int k = 0; k < 8; ++k) m.fhx[k * N + i] = f[k];
-    gather8(m.yd, nl, vel);
-    fb_force_axis(hg, vel, coefficient, f);
+    for (int a = 0; a < 3; ++a) {
+        gather8(vels[a], nl, vel);
+        fb_force_axis(hg, vel, coefficient, f);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) m.fhy[k * N + i] = f[k];
-    gather8(m.zd, nl, vel);
-    fb_force_axis(hg, vel, coefficient, f);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) m.fhz[k * N + i] = f[k];
+        for (int k = 0; k < 8; ++k) {
+#if LULESH_EXACT
+            outs[a][k * N + i] = f[k];
+#else
+            outs[a][k * N + i] = outs[a][k * N + i] + f[k];
+#endif
+        }
+    }
 }
 
 // Node n: gather in CSR order, stress then hourglass per corner
@@ -97,12 +113,18 @@ __device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt) {
     for (int j = b; j < e; ++j) {
         const int c = LD(m.nodeElemCornerList + j);
         const size_t idx = (size_t)(c & 7) * N + (size_t)(c >> 3);
+#if LULESH_EXACT
         fx += LD(m.fsx + idx);
         fx += LD(m.fhx + idx);
         fy += LD(m.fsy + idx);
         fy += LD(m.fhy + idx);
         fz += LD(m.fsz + idx);
         fz += LD(m.fhz + idx);
+#else
+        fx += LD(m.fsx + idx);  // stress + hourglass, combined by forces_elem
+        fy += LD(m.fsy + idx);
+        fz += LD(m.fsz + idx);
+#endif
     }
     node_update(m, n, fx, fy, fz, dt);
 }

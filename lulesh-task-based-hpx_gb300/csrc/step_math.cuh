@@ -173,6 +173,50 @@ __device__ __forceinline__ R quot(R a, R b) {
 #endif
 }
 
+// Comparisons. On GB300 a double compare (DSETP) occupies the FP64 pipe,
+// which issues at 1/60 the integer rate. The fast variants compare the
+// doubles' bit patterns on the integer pipe instead: positive doubles order
+// like their 64-bit patterns, negative ones in reverse. For non-NaN inputs
+// these give the IEEE results, except that -0 may compare below +0 (a test
+// that then stores the constant turns a -0 into +0). The exact variant keeps
+// the IEEE compares.
+#if LULESH_EXACT
+__device__ __forceinline__ bool f_lt(double x, double c) { return x < c; }
+__device__ __forceinline__ bool f_le(double x, double c) { return x <= c; }
+__device__ __forceinline__ bool f_gt(double x, double c) { return x > c; }
+__device__ __forceinline__ bool f_ge(double x, double c) { return x >= c; }
+__device__ __forceinline__ bool f_abs_lt(double x, double c) { return fabs(x) < c; }
+__device__ __forceinline__ bool f_is_zero(double x) { return x == 0.0; }
+#else
+constexpr long long kMag = 0x7fffffffffffffffLL;
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool f_lt(double x, double c) {
+    const long long bx = dbits(x), bc = dbits(c);
+    return bc >= 0 ? bx < bc : (bx < 0 && (bx & kMag) > (bc & kMag));
+}
+__device__ __forceinline__ bool f_le(double x, double c) {
+    const long long bx = dbits(x), bc = dbits(c);
+    return bc >= 0 ? bx <= bc : (bx < 0 && (bx & kMag) >= (bc & kMag));
+}
+__device__ __forceinline__ bool f_gt(double x, double c) { return !f_le(x, c); }
+__device__ __forceinline__ bool f_ge(double x, double c) { return !f_lt(x, c); }
+__device__ __forceinline__ bool f_abs_lt(double x, double c) { return (dbits(x) & kMag) < dbits(c); }
+__device__ __forceinline__ bool f_is_zero(double x) { return (dbits(x) & kMag) == 0; }
+#endif
+// two variables (the limiter); floats compare on the float pipe
+__device__ __forceinline__ bool f_vlt(double a, double b) {
+#if LULESH_EXACT
+    return a < b;
+#else
+    const long long ba = dbits(a), bb = dbits(b);
+    const long long ka = ba ^ ((ba >> 63) & kMag), kb = bb ^ ((bb >> 63) & kMag);
+    return ka < kb;
+#endif
+}
+__device__ __forceinline__ bool f_vlt(float a, float b) { return a < b; }
+__device__ __forceinline__ bool f_lt(float x, float c) { return x < c; }
+__device__ __forceinline__ bool f_gt(float x, float c) { return x > c; }
+
 __device__ __forceinline__ double recip_sqrt(double b) { return rsqrt(b); }
 __device__ __forceinline__ float recip_sqrt(float b) { return rsqrtf(b); }
 
@@ -190,21 +234,44 @@ __device__ __forceinline__ R div_sqrt(R a, R b) {
 // The reference's factors 0.5 (bisectors) and 0.25 (area) are left out: the
 // normals come out scaled by exactly 16, and callers scale the stress by
 // 1/16 instead. Powers of two commute with rounding, so this is bit-exact.
-template <int A, int B, int C, int D, class R>
+// INIT is a bit mask over the corners A..D (bit 0 = A): a set bit stores
+// the face's area vector into that corner instead of adding it (the fast
+// variants start each corner from its first face rather than from 0).
+template <int A, int B, int C, int D, int INIT, class R>
 __device__ __forceinline__ void face_normal(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
                                             const R z[8]) {
+#if LULESH_EXACT
     const R bisX0 = (x[D] + x[C] - x[B] - x[A]);
     const R bisY0 = (y[D] + y[C] - y[B] - y[A]);
     const R bisZ0 = (z[D] + z[C] - z[B] - z[A]);
     const R bisX1 = (x[C] + x[B] - x[D] - x[A]);
     const R bisY1 = (y[C] + y[B] - y[D] - y[A]);
     const R bisZ1 = (z[C] + z[B] - z[D] - z[A]);
+#else
+    // the two bisectors share the diagonals (C - A) and (D - B)
+    const R sx = x[C] - x[A], tx = x[D] - x[B];
+    const R sy = y[C] - y[A], ty = y[D] - y[B];
+    const R sz = z[C] - z[A], tz = z[D] - z[B];
+    const R bisX0 = sx + tx, bisX1 = sx - tx;
+    const R bisY0 = sy + ty, bisY1 = sy - ty;
+    const R bisZ0 = sz + tz, bisZ1 = sz - tz;
+#endif
     const R ax = (bisY0 * bisZ1 - bisZ0 * bisY1);
     const R ay = (bisZ0 * bisX1 - bisX0 * bisZ1);
     const R az = (bisX0 * bisY1 - bisY0 * bisX1);
-    nx[A] += ax; nx[B] += ax; nx[C] += ax; nx[D] += ax;
-    ny[A] += ay; ny[B] += ay; ny[C] += ay; ny[D] += ay;
-    nz[A] += az; nz[B] += az; nz[C] += az; nz[D] += az;
+    const int c[4] = {A, B, C, D};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (INIT & (1 << k)) {
+            nx[c[k]] = ax;
+            ny[c[k]] = ay;
+            nz[c[k]] = az;
+        } else {
+            nx[c[k]] += ax;
+            ny[c[k]] += ay;
+            nz[c[k]] += az;
+        }
+    }
 }
 
 // CalcElemNodeNormals (lulesh.cc:413-451), faces in the reference's order;
@@ -212,14 +279,21 @@ __device__ __forceinline__ void face_normal(R nx[8], R ny[8], R nz[8], const R x
 template <class R>
 __device__ __forceinline__ void node_normals(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
                                              const R z[8]) {
+#if LULESH_EXACT
 #pragma unroll
     for (int k = 0; k < 8; ++k) nx[k] = ny[k] = nz[k] = R(0.0);
-    face_normal<0, 1, 2, 3>(nx, ny, nz, x, y, z);
-    face_normal<0, 4, 5, 1>(nx, ny, nz, x, y, z);
-    face_normal<1, 5, 6, 2>(nx, ny, nz, x, y, z);
-    face_normal<2, 6, 7, 3>(nx, ny, nz, x, y, z);
-    face_normal<3, 7, 4, 0>(nx, ny, nz, x, y, z);
-    face_normal<4, 7, 6, 5>(nx, ny, nz, x, y, z);
+    face_normal<0, 1, 2, 3, 0>(nx, ny, nz, x, y, z);
+    face_normal<0, 4, 5, 1, 0>(nx, ny, nz, x, y, z);
+    face_normal<1, 5, 6, 2, 0>(nx, ny, nz, x, y, z);
+    face_normal<2, 6, 7, 3, 0>(nx, ny, nz, x, y, z);
+#else
+    face_normal<0, 1, 2, 3, 0xF>(nx, ny, nz, x, y, z);  // first touch of corners 0-3
+    face_normal<0, 4, 5, 1, 0x6>(nx, ny, nz, x, y, z);  // of corners 4, 5
+    face_normal<1, 5, 6, 2, 0x4>(nx, ny, nz, x, y, z);  // of corner 6
+    face_normal<2, 6, 7, 3, 0x4>(nx, ny, nz, x, y, z);  // of corner 7
+#endif
+    face_normal<3, 7, 4, 0, 0>(nx, ny, nz, x, y, z);
+    face_normal<4, 7, 6, 5, 0>(nx, ny, nz, x, y, z);
 }
 
 // VoluDer (lulesh.cc:468-491) for corner K from the corners P0..P5.
@@ -281,6 +355,30 @@ __device__ __forceinline__ R hourmod(const R v[8]) {
            v[6] * R(gamma_sign(M, 6)) + v[7] * R(gamma_sign(M, 7));
 }
 
+// All four mode sums of one coordinate with shared pair sums and differences
+// (18 adds instead of 28); a different summation order than the reference,
+// so fast variants only.
+template <class R>
+__device__ __forceinline__ void hourmod4(const R v[8], R h[4]) {
+    const R a01 = v[0] + v[1], a23 = v[2] + v[3], a45 = v[4] + v[5], a67 = v[6] + v[7];
+    const R d01 = v[0] - v[1], d23 = v[2] - v[3], d45 = v[4] - v[5], d67 = v[6] - v[7];
+    const R p = d01 + d23, q = d45 + d67;
+    h[0] = (a01 - a23) - (a45 - a67);  // (+ + - - - - + +)
+    h[1] = (d01 - d23) - (d45 - d67);  // (+ - - + - + + -)
+    h[2] = p + q;                      // (+ - + - + - + -)
+    h[3] = q - p;                      // (- + - + + - + -)
+}
+
+// Hourglass shape vectors of mode M (lulesh.cc:988-1023), from the mode sums
+// hx, hy, hz of the coordinates.
+template <int M, class R>
+__device__ __forceinline__ void hourgam_mode_h(R hg[8][4], R hx, R hy, R hz, const R dvdx[8],
+                                               const R dvdy[8], const R dvdz[8], R volinv) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        hg[k][M] = R(gamma_sign(M, k)) - volinv * (dvdx[k] * hx + dvdy[k] * hy + dvdz[k] * hz);
+}
+
 // Hourglass shape vectors of mode M (lulesh.cc:988-1023).
 template <int M, class R>
 __device__ __forceinline__ void hourgam_mode(R hg[8][4], const R x[8], const R y[8], const R z[8],
@@ -298,13 +396,22 @@ template <class R>
 __device__ __forceinline__ void hourgam_all(R hg[8][4], const R x[8], const R y[8], const R z[8],
                                             const R dvdx[8], const R dvdy[8], const R dvdz[8],
                                             R volinv) {
-#if !LULESH_EXACT
-    volinv = volinv * (R(1.0) / R(12.0));
-#endif
+#if LULESH_EXACT
     hourgam_mode<0>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
     hourgam_mode<1>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
     hourgam_mode<2>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
     hourgam_mode<3>(hg, x, y, z, dvdx, dvdy, dvdz, volinv);
+#else
+    volinv = volinv * (R(1.0) / R(12.0));
+    R hx[4], hy[4], hz[4];
+    hourmod4(x, hx);
+    hourmod4(y, hy);
+    hourmod4(z, hz);
+    hourgam_mode_h<0>(hg, hx[0], hy[0], hz[0], dvdx, dvdy, dvdz, volinv);
+    hourgam_mode_h<1>(hg, hx[1], hy[1], hz[1], dvdx, dvdy, dvdz, volinv);
+    hourgam_mode_h<2>(hg, hx[2], hy[2], hz[2], dvdx, dvdy, dvdz, volinv);
+    hourgam_mode_h<3>(hg, hx[3], hy[3], hz[3], dvdx, dvdy, dvdz, volinv);
+#endif
 }
 
 // CalcElemFBHourglassForce for one axis (lulesh.cc:527-562).
@@ -464,10 +571,10 @@ __device__ __forceinline__ R limiter(const R* __restrict__ dv, int i, int bm, in
     R phi = R(.5) * (delvm + delvp);
     delvm *= mult;
     delvp *= mult;
-    if (delvm < phi) phi = delvm;
-    if (delvp < phi) phi = delvp;
-    if (phi < R(0.)) phi = R(0.);
-    if (phi > max_slope) phi = max_slope;
+    if (f_vlt(delvm, phi)) phi = delvm;
+    if (f_vlt(delvp, phi)) phi = delvp;
+    if (f_lt(phi, R(0.))) phi = R(0.);
+    if (f_gt(phi, max_slope)) phi = max_slope;
     return phi;
 }
 
@@ -488,7 +595,7 @@ __device__ __forceinline__ void q_terms(const Mesh& m, int i, const R* dvxi, con
     const R phizeta = limiter(dvzeta, i, bc & ZETA_M, bc & ZETA_P, ZETA_M_SYMM, ZETA_M_COMM,
                               LD(m.lzetam + i), ZETA_P_SYMM, ZETA_P_COMM, LD(m.lzetap + i), mult,
                               slope);
-    if (vdov > 0.) {
+    if (f_gt(vdov, 0.)) {
         ql = 0.;
         qq = 0.;
         return;
@@ -496,9 +603,9 @@ __device__ __forceinline__ void q_terms(const Mesh& m, int i, const R* dvxi, con
     R dxi = LD(dvxi + i) * LD(dxxi + i);
     R deta = LD(dveta + i) * LD(dxeta + i);
     R dzeta = LD(dvzeta + i) * LD(dxzeta + i);
-    if (dxi > R(0.)) dxi = R(0.);
-    if (deta > R(0.)) deta = R(0.);
-    if (dzeta > R(0.)) dzeta = R(0.);
+    if (f_gt(dxi, R(0.))) dxi = R(0.);
+    if (f_gt(deta, R(0.))) deta = R(0.);
+    if (f_gt(dzeta, R(0.))) dzeta = R(0.);
     const R rho = R(quot(LD(m.elemMass + i), LD(m.volo + i) * vnew));
     const R qlin = -R(P.qlc_monoq) * rho *
                    (dxi * (R(1.) - phixi) + deta * (R(1.) - phieta) + dzeta * (R(1.) - phizeta));
@@ -516,16 +623,16 @@ __device__ __forceinline__ double eos_pressure(double& bvc, double& pbvc, double
     bvc = cls * (comp + 1.0);
     pbvc = cls;
     double nv = bvc * e;
-    if (fabs(nv) < P.p_cut || vnewc >= P.eosvmax) nv = 0.0;
-    if (nv < P.pmin) nv = P.pmin;
+    if (f_abs_lt(nv, P.p_cut) || f_ge(vnewc, P.eosvmax)) nv = 0.0;
+    if (f_lt(nv, P.pmin)) nv = P.pmin;
     return nv;
 }
 
 __device__ __forceinline__ double ss_guard(double ssc) {
 #if LULESH_EXACT
-    return (ssc <= .1111111e-36) ? .3333333e-18 : sqrt(ssc);
+    return f_le(ssc, .1111111e-36) ? .3333333e-18 : sqrt(ssc);
 #else
-    return (ssc <= .1111111e-36) ? .3333333e-18 : ssc * rsqrt(ssc);  // sqrt, one rounding more
+    return f_le(ssc, .1111111e-36) ? .3333333e-18 : ssc * rsqrt(ssc);  // sqrt, one rounding more
 #endif
 }
 
@@ -559,18 +666,18 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
         double comp = rcp(vnewc) - 1.;
         const double vchalf = vnewc - delvc * .5;
         double compHalf = rcp(vchalf) - 1.;
-        if (P.eosvmin != 0. && vnewc <= P.eosvmin) compHalf = comp;
-        if (P.eosvmax != 0.0 && vnewc >= P.eosvmax) {
+        if (P.eosvmin != 0. && f_le(vnewc, P.eosvmin)) compHalf = comp;
+        if (P.eosvmax != 0.0 && f_ge(vnewc, P.eosvmax)) {
             p_old = 0.;
             comp = 0.;
             compHalf = 0.;
         }
         // predictor
         e_new = e_old - 0.5 * delvc * (p_old + q_old) LULESH_PLUS_ZERO_WORK;
-        if (e_new < P.emin) e_new = P.emin;
+        if (f_lt(e_new, P.emin)) e_new = P.emin;
         const double pHalf = eos_pressure(bvc, pbvc, e_new, compHalf, vnewc, P);
         const double vhalf = rcp(1. + compHalf);
-        if (delvc > 0.) {
+        if (f_gt(delvc, 0.)) {
             q_new = 0.;
         } else {
             const double ssc = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vhalf * vhalf * bvc * pHalf), P));
@@ -578,14 +685,14 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
         }
         e_new = e_new + 0.5 * delvc * (3.0 * (p_old + q_old) - 4.0 * (pHalf + q_new));
         e_new = e_new LULESH_PLUS_ZERO_WORK;
-        if (fabs(e_new) < P.e_cut) e_new = 0.0;
-        if (e_new < P.emin) e_new = P.emin;
+        if (f_abs_lt(e_new, P.e_cut)) e_new = 0.0;
+        if (f_lt(e_new, P.emin)) e_new = P.emin;
         p_new = eos_pressure(bvc, pbvc, e_new, comp, vnewc, P);
         // corrector
         {
             const double sixth = 1.0 / 6.0;
             double q_tilde;
-            if (delvc > 0.) {
+            if (f_gt(delvc, 0.)) {
                 q_tilde = 0.;
             } else {
                 const double ssc = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vnewc * vnewc * bvc * p_new), P));
@@ -593,14 +700,14 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
             }
             e_new = e_new -
                     (7.0 * (p_old + q_old) - 8.0 * (pHalf + q_new) + (p_new + q_tilde)) * delvc * sixth;
-            if (fabs(e_new) < P.e_cut) e_new = 0.;
-            if (e_new < P.emin) e_new = P.emin;
+            if (f_abs_lt(e_new, P.e_cut)) e_new = 0.;
+            if (f_lt(e_new, P.emin)) e_new = P.emin;
         }
         p_new = eos_pressure(bvc, pbvc, e_new, comp, vnewc, P);
-        if (delvc <= 0.) {
+        if (f_le(delvc, 0.)) {
             const double ssc = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vnewc * vnewc * bvc * p_new), P));
             q_new = (ssc * ql_old + qq_old);
-            if (fabs(q_new) < P.q_cut) q_new = 0.;
+            if (f_abs_lt(q_new, P.q_cut)) q_new = 0.;
         }
     }
     const double sst = ss_guard(over_rho<UNIT_RHO>((pbvc * e_new + vnewc * vnewc * bvc * p_new), P));
@@ -619,10 +726,10 @@ __device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc
 // folded into running minima; vdov == 0 elements do not constrain.
 __device__ __forceinline__ void dt_constraints(const lulesh_params& P, double ss, double vdov,
                                                double arealg, double& dtc, double& dth) {
-    if (vdov == 0.0) return;
+    if (f_is_zero(vdov)) return;
     const double qqc2 = 64.0 * P.qqc * P.qqc;
     double dtf = ss * ss;
-    if (vdov < 0.0) dtf += qqc2 * arealg * arealg * vdov * vdov;
+    if (f_lt(vdov, 0.0)) dtf += qqc2 * arealg * arealg * vdov * vdov;
     dtf = div_sqrt(arealg, dtf);  // arealg / sqrt(dtf)
     dtc = fmin(dtc, dtf);
     dth = fmin(dth, quot(P.dvovmax, fabs(vdov) + 1.e-20));
@@ -710,11 +817,11 @@ __device__ __forceinline__ void node_update(const Mesh& m, int n, double fx, dou
     m.zdd[n] = az;
     const double u_cut = m.prm.u_cut;
     double vx = m.xd[n] + ax * dt;
-    if (fabs(vx) < u_cut) vx = 0.0;
+    if (f_abs_lt(vx, u_cut)) vx = 0.0;
     double vy = m.yd[n] + ay * dt;
-    if (fabs(vy) < u_cut) vy = 0.0;
+    if (f_abs_lt(vy, u_cut)) vy = 0.0;
     double vz = m.zd[n] + az * dt;
-    if (fabs(vz) < u_cut) vz = 0.0;
+    if (f_abs_lt(vz, u_cut)) vz = 0.0;
     m.xd[n] = vx;
     m.yd[n] = vy;
     m.zd[n] = vz;
