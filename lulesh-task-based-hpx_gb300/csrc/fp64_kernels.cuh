@@ -144,7 +144,7 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     const double vold = m.v[i];
     m.vnew[i] = relv;
     m.delv[i] = relv - vold;
-    m.arealg[i] = div_sqrt(4.0 * volume, max_face_area(x, y, z));
+    m.arealg[i] = char_length(x, y, z, volume);
 
     gather8(m.xd, nl, xv);
     gather8(m.yd, nl, yv);

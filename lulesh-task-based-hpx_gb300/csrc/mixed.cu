@@ -150,7 +150,7 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     rel8(m.pxp, nl, x);
     rel8(m.pyp, nl, y);
     rel8(m.pzp, nl, z);
-    m.arealg[i] = double(div_sqrt(4.0f * float(volume), max_face_area(x, y, z)));
+    m.arealg[i] = double(char_length(x, y, z, float(volume)));
     rel8(m.vxp, nl, xv);
     rel8(m.vyp, nl, yv);
     rel8(m.vzp, nl, zv);

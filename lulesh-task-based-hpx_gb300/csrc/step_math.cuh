@@ -455,6 +455,45 @@ __device__ __forceinline__ R max_ref(R a, R cl) {
     return (a < cl) ? cl : a;  // std::max(a, cl)
 }
 
+#if !LULESH_EXACT
+// max of two non-negative values; doubles on the integer pipe
+__device__ __forceinline__ double nonneg_max(double a, double b) {
+    return __longlong_as_double(max(dbits(a), dbits(b)));
+}
+__device__ __forceinline__ float nonneg_max(float a, float b) { return fmaxf(a, b); }
+
+// |s x t|^2 for the face diagonals s = C - A, t = D - B: a quarter of the
+// reference's face measure (with f = s - t, g = s + t, Lagrange's identity
+// gives |f|^2 |g|^2 - (f.g)^2 = |f x g|^2 = 4 |s x t|^2).
+template <int A, int B, int C, int D, class R>
+__device__ __forceinline__ R face_cross2(const R x[8], const R y[8], const R z[8]) {
+    const R sx = x[C] - x[A], sy = y[C] - y[A], sz = z[C] - z[A];
+    const R tx = x[D] - x[B], ty = y[D] - y[B], tz = z[D] - z[B];
+    const R cx = sy * tz - sz * ty, cy = sz * tx - sx * tz, cz = sx * ty - sy * tx;
+    return cx * cx + cy * cy + cz * cz;
+}
+#endif
+
+// Characteristic length 4 V / sqrt(largest face measure)
+// (CalcElemCharacteristicLength, lulesh.cc:696-729).
+template <class R>
+__device__ __forceinline__ R max_face_area(const R x[8], const R y[8], const R z[8]);
+
+template <class R>
+__device__ __forceinline__ R char_length(const R x[8], const R y[8], const R z[8], R volume) {
+#if LULESH_EXACT
+    return div_sqrt(R(4.0) * volume, max_face_area(x, y, z));
+#else
+    R cl = face_cross2<0, 1, 2, 3>(x, y, z);
+    cl = nonneg_max(cl, face_cross2<4, 5, 6, 7>(x, y, z));
+    cl = nonneg_max(cl, face_cross2<0, 1, 5, 4>(x, y, z));
+    cl = nonneg_max(cl, face_cross2<1, 2, 6, 5>(x, y, z));
+    cl = nonneg_max(cl, face_cross2<2, 3, 7, 6>(x, y, z));
+    cl = nonneg_max(cl, face_cross2<3, 0, 4, 7>(x, y, z));
+    return div_sqrt(R(2.0) * volume, cl);  // 4 V / sqrt(4 cl)
+#endif
+}
+
 // Largest face measure of CalcElemCharacteristicLength (lulesh.cc:696-729);
 // the characteristic length is 4 V / sqrt(of it).
 template <class R>
@@ -472,9 +511,59 @@ __device__ __forceinline__ R max_face_area(const R x[8], const R y[8], const R z
 // Monotonic-Q gradients of CalcMonotonicQGradientsForElemsTask
 // (lulesh.cc:1341-1416). vol = volo * vnew. Outputs
 // g[0..2] = delv_xi, delv_eta, delv_zeta and g[3..5] = delx_xi, delx_eta, delx_zeta.
+#if !LULESH_EXACT
+// 4 x the j, i, k direction differences of CalcMonotonicQGradients
+// (lulesh.cc:1341-1349) from 8 shared pair sums.
+template <class R>
+__device__ __forceinline__ void dirs4(const R v[8], R& dj, R& di, R& dk) {
+    const R a01 = v[0] + v[1], a23 = v[2] + v[3], a45 = v[4] + v[5], a67 = v[6] + v[7];
+    const R a12 = v[1] + v[2], a56 = v[5] + v[6], a03 = v[0] + v[3], a47 = v[4] + v[7];
+    dj = (a23 + a67) - (a01 + a45);
+    di = (a12 + a56) - (a03 + a47);
+    dk = (a45 + a67) - (a01 + a23);
+}
+#endif
+
 template <class R>
 __device__ __forceinline__ void q_gradients(const R x[8], const R y[8], const R z[8], const R xv[8],
                                             const R yv[8], const R zv[8], R vol, R g[6]) {
+#if !LULESH_EXACT
+    // Fast variants: the differences come 4x too large (D = 4d, V = 4dv), so
+    // a cross product A = 16a: delx = 16 vol / sqrt(|A|^2 + 256 ptiny) and
+    // delv = (A . V) norm / 64, with all scalings powers of two.
+    {
+        R Xj, Xi, Xk, Yj, Yi, Yk, Zj, Zi, Zk, xj, xi, xk, yj, yi, yk, zj, zi, zk;
+        dirs4(x, Xj, Xi, Xk);
+        dirs4(y, Yj, Yi, Yk);
+        dirs4(z, Zj, Zi, Zk);
+        dirs4(xv, xj, xi, xk);
+        dirs4(yv, yj, yi, yk);
+        dirs4(zv, zj, zi, zk);
+        const R pt = R(256.0) * R(1.e-36);
+        const R vol16 = R(16.0) * vol;
+        const R n64 = rcp(vol + R(1.e-36)) * R(0.015625);
+        R ax, ay, az;
+        // zeta: i cross j, velocities along k
+        ax = Yi * Zj - Zi * Yj;
+        ay = Zi * Xj - Xi * Zj;
+        az = Xi * Yj - Yi * Xj;
+        g[5] = vol16 * recip_sqrt(ax * ax + ay * ay + az * az + pt);
+        g[2] = (ax * xk + ay * yk + az * zk) * n64;
+        // xi: j cross k, velocities along i
+        ax = Yj * Zk - Zj * Yk;
+        ay = Zj * Xk - Xj * Zk;
+        az = Xj * Yk - Yj * Xk;
+        g[3] = vol16 * recip_sqrt(ax * ax + ay * ay + az * az + pt);
+        g[0] = (ax * xi + ay * yi + az * zi) * n64;
+        // eta: k cross i, velocities along j
+        ax = Yk * Zi - Zk * Yi;
+        ay = Zk * Xi - Xk * Zi;
+        az = Xk * Yi - Yk * Xi;
+        g[4] = vol16 * recip_sqrt(ax * ax + ay * ay + az * az + pt);
+        g[1] = (ax * xj + ay * yj + az * zj) * n64;
+        return;
+    }
+#endif
     const R ptiny = R(1.e-36);
     const R q = R(0.25), mq = R(-0.25);
     const R norm = rcp(vol + ptiny);
