@@ -47,15 +47,15 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     // stress (InitIntegrateStressForElemsTask, lulesh.cc:787-836)
     {
         const double sig = -LD(m.p + i) - LD(m.q + i);
-        if (jac_det(jacobian(x, y, z)) == 0) raise_error(m.result, i, PHASE_FORCES);
+        if (jacobian_singular(x, y, z)) raise_error(m.result, i, PHASE_FORCES);
         double nx[8], ny[8], nz[8];
-        node_normals(nx, ny, nz, x, y, z);   // 16 x the normals
-        const double sig16 = sig * 0.0625;  // exact: a power of two
+        node_normals(nx, ny, nz, x, y, z);  // 16 (exact) or 8 (fast) x the normals
+        const double sigs = sig * kInvNormalScale;  // a power of two: exact
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            m.fsx[k * N + i] = -(sig16 * nx[k]);
-            m.fsy[k * N + i] = -(sig16 * ny[k]);
-            m.fsz[k * N + i] = -(sig16 * nz[k]);
+            m.fsx[k * N + i] = -(sigs * nx[k]);
+            m.fsy[k * N + i] = -(sigs * ny[k]);
+            m.fsz[k * N + i] = -(sigs * nz[k]);
         }
     }
 
@@ -149,24 +149,14 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     gather8(m.xd, nl, xv);
     gather8(m.yd, nl, yv);
     gather8(m.zd, nl, zv);
-    {
-        double g[6];
-        q_gradients(x, y, z, xv, yv, zv, LD(m.volo + i) * relv, g);
-        m.dvxi[i] = g[0];
-        m.dveta[i] = g[1];
-        m.dvzeta[i] = g[2];
-        m.dxxi[i] = g[3];
-        m.dxeta[i] = g[4];
-        m.dxzeta[i] = g[5];
-    }
-    const double dt2 = 0.5 * dt;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        x[k] -= dt2 * xv[k];
-        y[k] -= dt2 * yv[k];
-        z[k] -= dt2 * zv[k];
-    }
-    m.vdov[i] = vel_grad_trace(x, y, z, xv, yv, zv);
+    double g[6];
+    m.vdov[i] = gradients_vdov(x, y, z, xv, yv, zv, LD(m.volo + i) * relv, 0.5 * dt, g);
+    m.dvxi[i] = g[0];
+    m.dveta[i] = g[1];
+    m.dvzeta[i] = g[2];
+    m.dxxi[i] = g[3];
+    m.dxeta[i] = g[4];
+    m.dxzeta[i] = g[5];
     update_volume(m, i, vold, relv);
 }
 

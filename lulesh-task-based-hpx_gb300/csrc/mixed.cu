@@ -61,9 +61,9 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
 
     float fx[8], fy[8], fz[8];
     {
-        // node_normals returns 16 x the normals: fold the 1/16 into the stress
-        const float sig = float(-LD(m.p + i) - LD(m.q + i)) * 0.0625f;
-        if (jac_det(jacobian(x, y, z)) == 0.0f) raise_error(m.result, i, PHASE_FORCES);
+        // node_normals returns 8 x the normals: fold the 1/8 into the stress
+        const float sig = float(-LD(m.p + i) - LD(m.q + i)) * float(kInvNormalScale);
+        if (jacobian_singular(x, y, z)) raise_error(m.result, i, PHASE_FORCES);
         float nx[8], ny[8], nz[8];
         node_normals(nx, ny, nz, x, y, z);
 #pragma unroll
@@ -154,24 +154,14 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     rel8(m.vxp, nl, xv);
     rel8(m.vyp, nl, yv);
     rel8(m.vzp, nl, zv);
-    {
-        float g[6];
-        q_gradients(x, y, z, xv, yv, zv, float(LD(m.volo + i) * relv), g);
-        m.gvxi[i] = g[0];
-        m.gveta[i] = g[1];
-        m.gvzeta[i] = g[2];
-        m.gxxi[i] = g[3];
-        m.gxeta[i] = g[4];
-        m.gxzeta[i] = g[5];
-    }
-    const float dt2 = float(0.5 * dt);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        x[k] -= dt2 * xv[k];
-        y[k] -= dt2 * yv[k];
-        z[k] -= dt2 * zv[k];
-    }
-    m.vdov[i] = double(vel_grad_trace(x, y, z, xv, yv, zv));
+    float g[6];
+    m.vdov[i] = double(gradients_vdov(x, y, z, xv, yv, zv, float(LD(m.volo + i) * relv), float(0.5 * dt), g));
+    m.gvxi[i] = g[0];
+    m.gveta[i] = g[1];
+    m.gvzeta[i] = g[2];
+    m.gxxi[i] = g[3];
+    m.gxeta[i] = g[4];
+    m.gxzeta[i] = g[5];
     update_volume(m, i, vold, relv);
 }
 

@@ -105,6 +105,56 @@ __device__ __forceinline__ R jac_det(const Jac<R>& j) {
     return R(8.) * (j.fjxet * cjxet + j.fjyet * cjyet + j.fjzet * cjzet);
 }
 
+#if !LULESH_EXACT
+// Direction sums of one coordinate (or velocity component) v from the four
+// body diagonals: d[0], d[1], d[2] along xi, eta, zeta are 8 times the centre
+// Jacobian entries fj?xi, fj?et, fj?ze (lulesh.cc:287-305) and 4 times the
+// Q-gradient differences d?i, d?j, d?k (lulesh.cc:1341-1349). Linear in v.
+template <class R>
+__device__ __forceinline__ void dirs(const R v[8], R d[3]) {
+    const R d60 = v[6] - v[0], d53 = v[5] - v[3], d71 = v[7] - v[1], d42 = v[4] - v[2];
+    const R u = d60 - d42, w = d53 - d71;
+    d[0] = u + w;
+    d[1] = u - w;
+    d[2] = (d60 + d42) + (d53 + d71);
+}
+
+// Cofactors c[a][b] of the 3x3 matrix J[a][b] (a = coordinate, b = direction;
+// c[0][0] is the reference's cjxxi, c[0][1] its cjxet, ...).
+template <class R>
+__device__ __forceinline__ void cofactors(const R J[3][3], R c[3][3]) {
+    c[0][0] = J[1][1] * J[2][2] - J[2][1] * J[1][2];
+    c[0][1] = J[2][0] * J[1][2] - J[1][0] * J[2][2];
+    c[0][2] = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+    c[1][0] = J[2][1] * J[0][2] - J[0][1] * J[2][2];
+    c[1][1] = J[0][0] * J[2][2] - J[2][0] * J[0][2];
+    c[1][2] = J[2][0] * J[0][1] - J[0][0] * J[2][1];
+    c[2][0] = J[0][1] * J[1][2] - J[1][1] * J[0][2];
+    c[2][1] = J[1][0] * J[0][2] - J[0][0] * J[1][2];
+    c[2][2] = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+}
+#endif
+
+// The reference's zero test on the centre Jacobian determinant of the force
+// phase (lulesh.cc:817-821). The fast variants test the determinant of 8
+// times the Jacobian in another summation order: zero for the same collapsed
+// elements, though a near-singular element may round differently.
+template <class R>
+__device__ __forceinline__ bool jacobian_singular(const R x[8], const R y[8], const R z[8]) {
+#if LULESH_EXACT
+    return jac_det(jacobian(x, y, z)) == R(0);
+#else
+    R J[3][3];
+    dirs(x, J[0]);
+    dirs(y, J[1]);
+    dirs(z, J[2]);
+    const R det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) +
+                  J[0][1] * (J[2][0] * J[1][2] - J[1][0] * J[2][2]) +
+                  J[0][2] * (J[1][0] * J[2][1] - J[2][0] * J[1][1]);
+    return det == R(0);
+#endif
+}
+
 // Shape-function derivatives b[a][0..3] (b[a][4..7] are their negatives,
 // lulesh.cc:337-364) and the determinant.
 template <class R>
@@ -234,67 +284,88 @@ __device__ __forceinline__ R div_sqrt(R a, R b) {
 // The reference's factors 0.5 (bisectors) and 0.25 (area) are left out: the
 // normals come out scaled by exactly 16, and callers scale the stress by
 // 1/16 instead. Powers of two commute with rounding, so this is bit-exact.
-// INIT is a bit mask over the corners A..D (bit 0 = A): a set bit stores
-// the face's area vector into that corner instead of adding it (the fast
-// variants start each corner from its first face rather than from 0).
-template <int A, int B, int C, int D, int INIT, class R>
+template <int A, int B, int C, int D, class R>
 __device__ __forceinline__ void face_normal(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
                                             const R z[8]) {
-#if LULESH_EXACT
     const R bisX0 = (x[D] + x[C] - x[B] - x[A]);
     const R bisY0 = (y[D] + y[C] - y[B] - y[A]);
     const R bisZ0 = (z[D] + z[C] - z[B] - z[A]);
     const R bisX1 = (x[C] + x[B] - x[D] - x[A]);
     const R bisY1 = (y[C] + y[B] - y[D] - y[A]);
     const R bisZ1 = (z[C] + z[B] - z[D] - z[A]);
-#else
-    // the two bisectors share the diagonals (C - A) and (D - B)
-    const R sx = x[C] - x[A], tx = x[D] - x[B];
-    const R sy = y[C] - y[A], ty = y[D] - y[B];
-    const R sz = z[C] - z[A], tz = z[D] - z[B];
-    const R bisX0 = sx + tx, bisX1 = sx - tx;
-    const R bisY0 = sy + ty, bisY1 = sy - ty;
-    const R bisZ0 = sz + tz, bisZ1 = sz - tz;
-#endif
     const R ax = (bisY0 * bisZ1 - bisZ0 * bisY1);
     const R ay = (bisZ0 * bisX1 - bisX0 * bisZ1);
     const R az = (bisX0 * bisY1 - bisY0 * bisX1);
     const int c[4] = {A, B, C, D};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        if (INIT & (1 << k)) {
-            nx[c[k]] = ax;
-            ny[c[k]] = ay;
-            nz[c[k]] = az;
-        } else {
-            nx[c[k]] += ax;
-            ny[c[k]] += ay;
-            nz[c[k]] += az;
-        }
+        nx[c[k]] += ax;
+        ny[c[k]] += ay;
+        nz[c[k]] += az;
     }
 }
 
-// CalcElemNodeNormals (lulesh.cc:413-451), faces in the reference's order;
-// the result is 16 times the reference's normals (see face_normal).
+#if !LULESH_EXACT
+// Half the bisector cross product of face A..D: with the diagonals
+// s = C - A and t = D - B the bisectors are s + t and s - t, and
+// (s + t) x (s - t) = 2 t x s.
+template <int A, int B, int C, int D, class R>
+__device__ __forceinline__ void face_txs(const R x[8], const R y[8], const R z[8], R a[3]) {
+    const R sx = x[C] - x[A], sy = y[C] - y[A], sz = z[C] - z[A];
+    const R tx = x[D] - x[B], ty = y[D] - y[B], tz = z[D] - z[B];
+    a[0] = ty * sz - tz * sy;
+    a[1] = tz * sx - tx * sz;
+    a[2] = tx * sy - ty * sx;
+}
+#endif
+
+// Scale of node_normals' result relative to the reference's normals; the
+// stress is multiplied by its inverse (a power of two).
+constexpr double kInvNormalScale = LULESH_EXACT ? 0.0625 : 0.125;
+
+// CalcElemNodeNormals (lulesh.cc:413-451). Exact variant: faces in the
+// reference's order, 16 times the reference's normals (see face_normal).
+// Fast variants: 8 times the normals, each corner the sum of its three
+// faces' t x s, with the four face pairs that two corners share added once:
+// corners 0,1 share faces 0123 and 0451, corners 2,3 faces 0123 and 2673,
+// corners 4,5 faces 0451 and 4765, corners 6,7 faces 2673 and 4765.
 template <class R>
 __device__ __forceinline__ void node_normals(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
                                              const R z[8]) {
 #if LULESH_EXACT
 #pragma unroll
     for (int k = 0; k < 8; ++k) nx[k] = ny[k] = nz[k] = R(0.0);
-    face_normal<0, 1, 2, 3, 0>(nx, ny, nz, x, y, z);
-    face_normal<0, 4, 5, 1, 0>(nx, ny, nz, x, y, z);
-    face_normal<1, 5, 6, 2, 0>(nx, ny, nz, x, y, z);
-    face_normal<2, 6, 7, 3, 0>(nx, ny, nz, x, y, z);
+    face_normal<0, 1, 2, 3>(nx, ny, nz, x, y, z);
+    face_normal<0, 4, 5, 1>(nx, ny, nz, x, y, z);
+    face_normal<1, 5, 6, 2>(nx, ny, nz, x, y, z);
+    face_normal<2, 6, 7, 3>(nx, ny, nz, x, y, z);
+    face_normal<3, 7, 4, 0>(nx, ny, nz, x, y, z);
+    face_normal<4, 7, 6, 5>(nx, ny, nz, x, y, z);
 #else
-    face_normal<0, 1, 2, 3, 0xF>(nx, ny, nz, x, y, z);  // first touch of corners 0-3
-    face_normal<0, 4, 5, 1, 0x6>(nx, ny, nz, x, y, z);  // of corners 4, 5
-    face_normal<1, 5, 6, 2, 0x4>(nx, ny, nz, x, y, z);  // of corner 6
-    face_normal<2, 6, 7, 3, 0x4>(nx, ny, nz, x, y, z);  // of corner 7
+    R f0[3], f1[3], f2[3], f3[3], f4[3], f5[3];
+    face_txs<0, 1, 2, 3>(x, y, z, f0);
+    face_txs<0, 4, 5, 1>(x, y, z, f1);
+    face_txs<1, 5, 6, 2>(x, y, z, f2);
+    face_txs<2, 6, 7, 3>(x, y, z, f3);
+    face_txs<3, 7, 4, 0>(x, y, z, f4);
+    face_txs<4, 7, 6, 5>(x, y, z, f5);
+    R* n[3] = {nx, ny, nz};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const R p01 = f0[c] + f1[c], p03 = f0[c] + f3[c];
+        const R p15 = f1[c] + f5[c], p35 = f3[c] + f5[c];
+        n[c][0] = p01 + f4[c];
+        n[c][1] = p01 + f2[c];
+        n[c][2] = p03 + f2[c];
+        n[c][3] = p03 + f4[c];
+        n[c][4] = p15 + f4[c];
+        n[c][5] = p15 + f2[c];
+        n[c][6] = p35 + f2[c];
+        n[c][7] = p35 + f4[c];
+    }
 #endif
-    face_normal<3, 7, 4, 0, 0>(nx, ny, nz, x, y, z);
-    face_normal<4, 7, 6, 5, 0>(nx, ny, nz, x, y, z);
 }
+
 
 // VoluDer (lulesh.cc:468-491) for corner K from the corners P0..P5.
 template <int K, int P0, int P1, int P2, int P3, int P4, int P5, class R>
@@ -369,14 +440,15 @@ __device__ __forceinline__ void hourmod4(const R v[8], R h[4]) {
     h[3] = q - p;                      // (- + - + + - + -)
 }
 
-// Hourglass shape vectors of mode M (lulesh.cc:988-1023), from the mode sums
-// hx, hy, hz of the coordinates.
+// Hourglass shape vectors of mode M (lulesh.cc:988-1023) from the mode sums
+// hx, hy, hz of the coordinates, already multiplied by volinv: three
+// multiply-adds per corner.
 template <int M, class R>
 __device__ __forceinline__ void hourgam_mode_h(R hg[8][4], R hx, R hy, R hz, const R dvdx[8],
-                                               const R dvdy[8], const R dvdz[8], R volinv) {
+                                               const R dvdy[8], const R dvdz[8]) {
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-        hg[k][M] = R(gamma_sign(M, k)) - volinv * (dvdx[k] * hx + dvdy[k] * hy + dvdz[k] * hz);
+        hg[k][M] = R(gamma_sign(M, k)) - dvdx[k] * hx - dvdy[k] * hy - dvdz[k] * hz;
 }
 
 // Hourglass shape vectors of mode M (lulesh.cc:988-1023).
@@ -407,10 +479,16 @@ __device__ __forceinline__ void hourgam_all(R hg[8][4], const R x[8], const R y[
     hourmod4(x, hx);
     hourmod4(y, hy);
     hourmod4(z, hz);
-    hourgam_mode_h<0>(hg, hx[0], hy[0], hz[0], dvdx, dvdy, dvdz, volinv);
-    hourgam_mode_h<1>(hg, hx[1], hy[1], hz[1], dvdx, dvdy, dvdz, volinv);
-    hourgam_mode_h<2>(hg, hx[2], hy[2], hz[2], dvdx, dvdy, dvdz, volinv);
-    hourgam_mode_h<3>(hg, hx[3], hy[3], hz[3], dvdx, dvdy, dvdz, volinv);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        hx[m] *= volinv;
+        hy[m] *= volinv;
+        hz[m] *= volinv;
+    }
+    hourgam_mode_h<0>(hg, hx[0], hy[0], hz[0], dvdx, dvdy, dvdz);
+    hourgam_mode_h<1>(hg, hx[1], hy[1], hz[1], dvdx, dvdy, dvdz);
+    hourgam_mode_h<2>(hg, hx[2], hy[2], hz[2], dvdx, dvdy, dvdz);
+    hourgam_mode_h<3>(hg, hx[3], hy[3], hz[3], dvdx, dvdy, dvdz);
 #endif
 }
 
@@ -511,59 +589,9 @@ __device__ __forceinline__ R max_face_area(const R x[8], const R y[8], const R z
 // Monotonic-Q gradients of CalcMonotonicQGradientsForElemsTask
 // (lulesh.cc:1341-1416). vol = volo * vnew. Outputs
 // g[0..2] = delv_xi, delv_eta, delv_zeta and g[3..5] = delx_xi, delx_eta, delx_zeta.
-#if !LULESH_EXACT
-// 4 x the j, i, k direction differences of CalcMonotonicQGradients
-// (lulesh.cc:1341-1349) from 8 shared pair sums.
-template <class R>
-__device__ __forceinline__ void dirs4(const R v[8], R& dj, R& di, R& dk) {
-    const R a01 = v[0] + v[1], a23 = v[2] + v[3], a45 = v[4] + v[5], a67 = v[6] + v[7];
-    const R a12 = v[1] + v[2], a56 = v[5] + v[6], a03 = v[0] + v[3], a47 = v[4] + v[7];
-    dj = (a23 + a67) - (a01 + a45);
-    di = (a12 + a56) - (a03 + a47);
-    dk = (a45 + a67) - (a01 + a23);
-}
-#endif
-
 template <class R>
 __device__ __forceinline__ void q_gradients(const R x[8], const R y[8], const R z[8], const R xv[8],
                                             const R yv[8], const R zv[8], R vol, R g[6]) {
-#if !LULESH_EXACT
-    // Fast variants: the differences come 4x too large (D = 4d, V = 4dv), so
-    // a cross product A = 16a: delx = 16 vol / sqrt(|A|^2 + 256 ptiny) and
-    // delv = (A . V) norm / 64, with all scalings powers of two.
-    {
-        R Xj, Xi, Xk, Yj, Yi, Yk, Zj, Zi, Zk, xj, xi, xk, yj, yi, yk, zj, zi, zk;
-        dirs4(x, Xj, Xi, Xk);
-        dirs4(y, Yj, Yi, Yk);
-        dirs4(z, Zj, Zi, Zk);
-        dirs4(xv, xj, xi, xk);
-        dirs4(yv, yj, yi, yk);
-        dirs4(zv, zj, zi, zk);
-        const R pt = R(256.0) * R(1.e-36);
-        const R vol16 = R(16.0) * vol;
-        const R n64 = rcp(vol + R(1.e-36)) * R(0.015625);
-        R ax, ay, az;
-        // zeta: i cross j, velocities along k
-        ax = Yi * Zj - Zi * Yj;
-        ay = Zi * Xj - Xi * Zj;
-        az = Xi * Yj - Yi * Xj;
-        g[5] = vol16 * recip_sqrt(ax * ax + ay * ay + az * az + pt);
-        g[2] = (ax * xk + ay * yk + az * zk) * n64;
-        // xi: j cross k, velocities along i
-        ax = Yj * Zk - Zj * Yk;
-        ay = Zj * Xk - Xj * Zk;
-        az = Xj * Yk - Yj * Xk;
-        g[3] = vol16 * recip_sqrt(ax * ax + ay * ay + az * az + pt);
-        g[0] = (ax * xi + ay * yi + az * zi) * n64;
-        // eta: k cross i, velocities along j
-        ax = Yk * Zi - Zk * Yi;
-        ay = Zk * Xi - Xk * Zi;
-        az = Xk * Yi - Yk * Xi;
-        g[4] = vol16 * recip_sqrt(ax * ax + ay * ay + az * az + pt);
-        g[1] = (ax * xj + ay * yj + az * zj) * n64;
-        return;
-    }
-#endif
     const R ptiny = R(1.e-36);
     const R q = R(0.25), mq = R(-0.25);
     const R norm = rcp(vol + ptiny);
@@ -634,6 +662,63 @@ __device__ __forceinline__ R vel_grad_trace(const R xh[8], const R yh[8], const 
     const R dzz = inv * (b[2][0] * (zv[0] - zv[6]) + b[2][1] * (zv[1] - zv[7]) +
                          b[2][2] * (zv[2] - zv[4]) + b[2][3] * (zv[3] - zv[5]));
     return dxx + dyy + dzz;
+}
+
+// Q gradients g (as q_gradients) and vdov, the trace of the velocity
+// gradient at the half-step geometry x - dt2 v (lulesh.cc:1221-1232), of one
+// element. Exact variant: the reference's two computations. Fast variants,
+// from the 18 direction sums X = dirs(x, y, z) and V = dirs(xv, yv, zv):
+//  * the Q-gradient cross products of directions i x j, j x k, k x i are the
+//    cofactor columns of X, and the sums are 4 times the reference's
+//    differences, so with C = cof(X) = 16 a: delx = 16 vol / sqrt(|C|^2 +
+//    256 ptiny) and delv = (C . V) / (64 (vol + ptiny));
+//  * the half-step Jacobian is J = X - dt2 V (dirs is linear) and the trace
+//    of V J^-1 is sum(cof(J) * V) / det(J); the 8x scale of J cancels.
+template <class R>
+__device__ __forceinline__ R gradients_vdov(const R x[8], const R y[8], const R z[8], const R xv[8],
+                                            const R yv[8], const R zv[8], R vol, R dt2, R g[6]) {
+#if LULESH_EXACT
+    q_gradients(x, y, z, xv, yv, zv, vol, g);
+    R xh[8], yh[8], zh[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        xh[k] = x[k] - dt2 * xv[k];
+        yh[k] = y[k] - dt2 * yv[k];
+        zh[k] = z[k] - dt2 * zv[k];
+    }
+    return vel_grad_trace(xh, yh, zh, xv, yv, zv);
+#else
+    R X[3][3], V[3][3], c[3][3];
+    dirs(x, X[0]);
+    dirs(y, X[1]);
+    dirs(z, X[2]);
+    dirs(xv, V[0]);
+    dirs(yv, V[1]);
+    dirs(zv, V[2]);
+    cofactors(X, c);
+    const R pt = R(256.0) * R(1.e-36);
+    const R vol16 = R(16.0) * vol;
+    const R n64 = rcp(vol + R(1.e-36)) * R(0.015625);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        g[3 + d] = vol16 * recip_sqrt(c[0][d] * c[0][d] + c[1][d] * c[1][d] + c[2][d] * c[2][d] + pt);
+        g[d] = (c[0][d] * V[0][d] + c[1][d] * V[1][d] + c[2][d] * V[2][d]) * n64;
+    }
+    R J[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) J[a][d] = X[a][d] - dt2 * V[a][d];
+    cofactors(J, c);
+    const R det = J[0][0] * c[0][0] + J[0][1] * c[0][1] + J[0][2] * c[0][2];
+    R num = c[0][0] * V[0][0];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (a + d > 0) num = num + c[a][d] * V[a][d];
+    return quot(num, det);
+#endif
 }
 
 // --- material ------------------------------------------------------------
