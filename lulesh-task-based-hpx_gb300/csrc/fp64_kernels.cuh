@@ -32,6 +32,7 @@ __device__ __forceinline__ double cube_root(double x) {
 #endif
 }
 
+#if LULESH_EXACT
 // Stress and hourglass corner forces of element i, stored separately
 // (corner-major) so that the node gather adds them in the reference's order
 // (lulesh.cc:849-856).
@@ -49,7 +50,7 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
         const double sig = -LD(m.p + i) - LD(m.q + i);
         if (jacobian_singular(x, y, z)) raise_error(m.result, i, PHASE_FORCES);
         double nx[8], ny[8], nz[8];
-        node_normals(nx, ny, nz, x, y, z);  // 16 (exact) or 8 (fast) x the normals
+        node_normals(nx, ny, nz, x, y, z);          // 16 x the normals
         const double sigs = sig * kInvNormalScale;  // a power of two: exact
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -71,38 +72,62 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
         volume_derivs(dvdx, dvdy, dvdz, x, y, z);
         hourgam_all(hg, x, y, z, dvdx, dvdy, dvdz, rcp(determ));
     }
-#if LULESH_EXACT
     const double coefficient =
         -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) / cube_root(determ);
-#else
-    // times the reciprocal cube root: one library call instead of cbrt + divide
-    const double coefficient = -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) * rcbrt(determ);
-#endif
     double vel[8], f[8];
-#if LULESH_EXACT
-    // separate hourglass arrays: the gather adds stress then hourglass
     double* outs[3] = {m.fhx, m.fhy, m.fhz};
-#else
-    // fast variant: one corner force per corner, stress + hourglass; the
-    // stress values written above are re-read from L2 and overwritten, so
-    // HBM sees a single 24-double store per element
-    double* outs[3] = {m.fsx, m.fsy, m.fsz};
-#endif
     const double* vels[3] = {m.xd, m.yd, m.zd};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         gather8(vels[a], nl, vel);
         fb_force_axis(hg, vel, coefficient, f);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-#if LULESH_EXACT
-            outs[a][k * N + i] = f[k];
-#else
-            outs[a][k * N + i] = outs[a][k * N + i] + f[k];
-#endif
-        }
+        for (int k = 0; k < 8; ++k) outs[a][k * N + i] = f[k];
     }
 }
+#else
+// Fast variant: stress plus hourglass corner force of element i summed in
+// registers and stored once (corner-major fsx, fsy, fsz). The stress force
+// (p + q) n enters through the six face vectors scaled by (p + q) / 8, each
+// corner's stress is the start of its hourglass multiply-add chain.
+// Elements that fail the determinant test store nothing: the step reports
+// the error and its state is not used.
+__device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
+    const size_t N = (size_t)m.numElem;
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    double x[8], y[8], z[8];
+    gather8(m.x, nl, x);
+    gather8(m.y, nl, y);
+    gather8(m.z, nl, z);
+    if (jacobian_singular(x, y, z)) raise_error(m.result, i, PHASE_FORCES);
+    const double determ = LD(m.volo + i) * LD(m.v + i);
+    if (f_le(determ, 0.0)) {
+        raise_error(m.result, i, PHASE_FORCES);
+        return;
+    }
+    double hg[8][4];
+    {
+        double dvdx[8], dvdy[8], dvdz[8];
+        volume_derivs(dvdx, dvdy, dvdz, x, y, z);
+        hourgam_all(hg, x, y, z, dvdx, dvdy, dvdz, rcp(determ));
+    }
+    double fa[6][3];
+    face_vectors(x, y, z, (LD(m.p + i) + LD(m.q + i)) * kInvNormalScale, fa);
+    const double coefficient = -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) * rcbrt_pos(determ);
+    double* outs[3] = {m.fsx, m.fsy, m.fsz};
+    const double* vels[3] = {m.xd, m.yd, m.zd};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double st[8], vel[8], f[8];
+        corner_sums(fa, a, st);
+        gather8(vels[a], nl, vel);
+        fb_force_axis_plus(hg, vel, coefficient, st, f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) outs[a][k * N + i] = f[k];
+    }
+}
+#endif
 
 // Node n: gather in CSR order, stress then hourglass per corner
 // (combineVolumeForcesTaskFunc, lulesh.cc:838-862), then the node update.

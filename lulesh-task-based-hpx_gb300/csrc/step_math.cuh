@@ -270,6 +270,24 @@ __device__ __forceinline__ bool f_gt(float x, float c) { return x > c; }
 __device__ __forceinline__ double recip_sqrt(double b) { return rsqrt(b); }
 __device__ __forceinline__ float recip_sqrt(float b) { return rsqrtf(b); }
 
+#if !LULESH_EXACT
+// Reciprocal cube root of a positive double (fast variants). Seed: the float
+// reciprocal cube root y of x rounded to float (documented within 1 float
+// ulp), so the residual r = 1 - x y^3 is below 2^-21 in magnitude. One
+// third-order correction from the binomial series
+//   x^(-1/3) = y (1 - r)^(-1/3) = y (1 + r/3 + 2 r^2/9 + 14 r^3/81 + ...)
+// leaves a truncation error below 2^-62; y^2 is exact (y has 24 significant
+// bits), so the result is within about one double ulp. Outside the float's
+// normal range the double library function is used instead.
+__device__ __forceinline__ double rcbrt_pos(double x) {
+    const float xf = __double2float_rn(x);
+    if (!(xf >= 1.17549435e-38f && xf <= 3.0e38f)) return rcbrt(x);
+    const double y = double(rcbrtf(xf));
+    const double r = fma(-x, (y * y) * y, 1.0);
+    return fma(y, r * fma(r, 2.0 / 9.0, 1.0 / 3.0), y);
+}
+#endif
+
 template <class R>
 __device__ __forceinline__ R div_sqrt(R a, R b) {
 #if LULESH_EXACT
@@ -323,12 +341,46 @@ __device__ __forceinline__ void face_txs(const R x[8], const R y[8], const R z[8
 // stress is multiplied by its inverse (a power of two).
 constexpr double kInvNormalScale = LULESH_EXACT ? 0.0625 : 0.125;
 
+#if !LULESH_EXACT
+// The six faces' t x s (face_txs) times scale, faces in the reference's
+// order 0123, 0451, 1562, 2673, 3740, 4765.
+template <class R>
+__device__ __forceinline__ void face_vectors(const R x[8], const R y[8], const R z[8], R scale,
+                                             R fa[6][3]) {
+    face_txs<0, 1, 2, 3>(x, y, z, fa[0]);
+    face_txs<0, 4, 5, 1>(x, y, z, fa[1]);
+    face_txs<1, 5, 6, 2>(x, y, z, fa[2]);
+    face_txs<2, 6, 7, 3>(x, y, z, fa[3]);
+    face_txs<3, 7, 4, 0>(x, y, z, fa[4]);
+    face_txs<4, 7, 6, 5>(x, y, z, fa[5]);
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) fa[f][c] *= scale;
+}
+
+// Component c of the corner sums of face_vectors: each corner adds its
+// three faces, and the four face pairs that two corners share are added
+// once (corners 0,1 share faces 0123 and 0451, corners 2,3 faces 0123 and
+// 2673, corners 4,5 faces 0451 and 4765, corners 6,7 faces 2673 and 4765).
+template <class R>
+__device__ __forceinline__ void corner_sums(const R fa[6][3], int c, R n[8]) {
+    const R p01 = fa[0][c] + fa[1][c], p03 = fa[0][c] + fa[3][c];
+    const R p15 = fa[1][c] + fa[5][c], p35 = fa[3][c] + fa[5][c];
+    n[0] = p01 + fa[4][c];
+    n[1] = p01 + fa[2][c];
+    n[2] = p03 + fa[2][c];
+    n[3] = p03 + fa[4][c];
+    n[4] = p15 + fa[4][c];
+    n[5] = p15 + fa[2][c];
+    n[6] = p35 + fa[2][c];
+    n[7] = p35 + fa[4][c];
+}
+#endif
+
 // CalcElemNodeNormals (lulesh.cc:413-451). Exact variant: faces in the
 // reference's order, 16 times the reference's normals (see face_normal).
-// Fast variants: 8 times the normals, each corner the sum of its three
-// faces' t x s, with the four face pairs that two corners share added once:
-// corners 0,1 share faces 0123 and 0451, corners 2,3 faces 0123 and 2673,
-// corners 4,5 faces 0451 and 4765, corners 6,7 faces 2673 and 4765.
+// Fast variants: 8 times the normals, the corner sums of the faces' t x s.
 template <class R>
 __device__ __forceinline__ void node_normals(R nx[8], R ny[8], R nz[8], const R x[8], const R y[8],
                                              const R z[8]) {
@@ -342,30 +394,18 @@ __device__ __forceinline__ void node_normals(R nx[8], R ny[8], R nz[8], const R 
     face_normal<3, 7, 4, 0>(nx, ny, nz, x, y, z);
     face_normal<4, 7, 6, 5>(nx, ny, nz, x, y, z);
 #else
-    R f0[3], f1[3], f2[3], f3[3], f4[3], f5[3];
-    face_txs<0, 1, 2, 3>(x, y, z, f0);
-    face_txs<0, 4, 5, 1>(x, y, z, f1);
-    face_txs<1, 5, 6, 2>(x, y, z, f2);
-    face_txs<2, 6, 7, 3>(x, y, z, f3);
-    face_txs<3, 7, 4, 0>(x, y, z, f4);
-    face_txs<4, 7, 6, 5>(x, y, z, f5);
-    R* n[3] = {nx, ny, nz};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const R p01 = f0[c] + f1[c], p03 = f0[c] + f3[c];
-        const R p15 = f1[c] + f5[c], p35 = f3[c] + f5[c];
-        n[c][0] = p01 + f4[c];
-        n[c][1] = p01 + f2[c];
-        n[c][2] = p03 + f2[c];
-        n[c][3] = p03 + f4[c];
-        n[c][4] = p15 + f4[c];
-        n[c][5] = p15 + f2[c];
-        n[c][6] = p35 + f2[c];
-        n[c][7] = p35 + f4[c];
-    }
+    R fa[6][3];
+    face_txs<0, 1, 2, 3>(x, y, z, fa[0]);
+    face_txs<0, 4, 5, 1>(x, y, z, fa[1]);
+    face_txs<1, 5, 6, 2>(x, y, z, fa[2]);
+    face_txs<2, 6, 7, 3>(x, y, z, fa[3]);
+    face_txs<3, 7, 4, 0>(x, y, z, fa[4]);
+    face_txs<4, 7, 6, 5>(x, y, z, fa[5]);
+    corner_sums(fa, 0, nx);
+    corner_sums(fa, 1, ny);
+    corner_sums(fa, 2, nz);
 #endif
 }
-
 
 // VoluDer (lulesh.cc:468-491) for corner K from the corners P0..P5.
 template <int K, int P0, int P1, int P2, int P3, int P4, int P5, class R>
@@ -514,6 +554,24 @@ __device__ __forceinline__ void fb_force_axis(const R hg[8][4], const R vel[8], 
         out[k] = hg[k][0] * h[0] + hg[k][1] * h[1] + hg[k][2] * h[2] + hg[k][3] * h[3];
 #endif
 }
+
+#if !LULESH_EXACT
+// fb_force_axis added to init[k] (the corner's stress force): four
+// multiply-adds per corner.
+template <class R>
+__device__ __forceinline__ void fb_force_axis_plus(const R hg[8][4], const R vel[8], R coefficient,
+                                                   const R init[8], R out[8]) {
+    R h[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+        h[m] = (hg[0][m] * vel[0] + hg[1][m] * vel[1] + hg[2][m] * vel[2] + hg[3][m] * vel[3] +
+                hg[4][m] * vel[4] + hg[5][m] * vel[5] + hg[6][m] * vel[6] + hg[7][m] * vel[7]) *
+               coefficient;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        out[k] = init[k] + hg[k][0] * h[0] + hg[k][1] * h[1] + hg[k][2] * h[2] + hg[k][3] * h[3];
+}
+#endif
 
 // AreaFace (lulesh.cc:678-692) of the face with corners A..D.
 template <int A, int B, int C, int D, class R>
@@ -810,19 +868,15 @@ __device__ __forceinline__ double ss_guard(double ssc) {
 #endif
 }
 
-// The reference's "+ 0.5 * work" terms add 0.5 * 0 (work is zero,
-// lulesh.cc:1749); adding +0 only turns a -0 into +0, so the fast variants
-// leave them out.
-#if LULESH_EXACT
-#define LULESH_PLUS_ZERO_WORK +0.5 * 0.0
-#else
-#define LULESH_PLUS_ZERO_WORK
-#endif
-
 // rep evaluations of EvalEOSAllInOneTask (lulesh.cc:1692-1871) for element i,
 // each from the saved state, then the sound speed and the save of
 // CalcSoundSpeedForElemsAndSaveTask (lulesh.cc:1873-1904). Returns ss.
 // UNIT_RHO: refdens == 1, so the divisions by it are identities.
+#if LULESH_EXACT
+// The reference's "+ 0.5 * work" terms add 0.5 * 0 (work is zero,
+// lulesh.cc:1749); adding +0 only turns a -0 into +0, so the fast variants
+// leave them out.
+#define LULESH_PLUS_ZERO_WORK +0.5 * 0.0
 template <bool UNIT_RHO>
 __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, int rep) {
     const lulesh_params& P = m.prm;
@@ -891,6 +945,81 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
     m.q[i] = q_new;
     return sst;
 }
+
+#else
+// Fast variants. The pressure coefficient bvc = 2/3 (comp + 1) is 2/3 / v
+// for comp = 1/v - 1, the reference's vhalf = 1 / (1 + compHalf) is vchalf
+// itself, and the sound-speed term v^2 bvc p is 2/3 v p: each pass forms two
+// reciprocals instead of three and each sound speed takes one multiply-add.
+// The eosvmin override (compHalf = comp) makes the half step use vnewc, and
+// the eosvmax override (comp = compHalf = 0) makes bvc = 2/3, vhalf = 1 and
+// the full-step term 2/3 vnewc^2 p. The repeat loop stays real work as in
+// the exact variant.
+__device__ __forceinline__ double pressure(double bvc, double e, double vnewc, const lulesh_params& P) {
+    double nv = bvc * e;
+    if (f_abs_lt(nv, P.p_cut) || f_ge(vnewc, P.eosvmax)) nv = 0.0;
+    if (f_lt(nv, P.pmin)) nv = P.pmin;
+    return nv;
+}
+
+template <bool UNIT_RHO>
+__device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, int rep) {
+    const lulesh_params& P = m.prm;
+    const double cls = 2.0 / 3.0;
+    double e_new = 0., p_new = 0., q_new = 0., vf = vnewc;
+    for (int r = 0; r < rep; ++r) {
+        asm volatile("" ::: "memory");
+        asm volatile("" : "+d"(vnewc));
+        const double e_old = m.e[i], delvc = m.delv[i], q_old = m.q[i];
+        double p_old = m.p[i];
+        const double qq_old = m.qq[i], ql_old = m.ql[i];
+        const double vchalf = vnewc - delvc * .5;
+        double bvcf = cls * rcp(vnewc), bvch = cls * rcp(vchalf);
+        double vh = vchalf;
+        vf = vnewc;
+        if (P.eosvmin != 0. && f_le(vnewc, P.eosvmin)) {
+            bvch = bvcf;
+            vh = vnewc;
+        }
+        if (P.eosvmax != 0.0 && f_ge(vnewc, P.eosvmax)) {
+            p_old = 0.;
+            bvcf = bvch = cls;
+            vh = 1.0;
+            vf = vnewc * vnewc;
+        }
+        const double pq_old = p_old + q_old;
+        // predictor
+        e_new = e_old - 0.5 * delvc * pq_old;
+        if (f_lt(e_new, P.emin)) e_new = P.emin;
+        const double pHalf = pressure(bvch, e_new, vnewc, P);
+        if (f_gt(delvc, 0.)) q_new = 0.;
+        else q_new = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vh * pHalf), P)) * ql_old + qq_old;
+        const double pq_half = pHalf + q_new;
+        e_new = e_new + 0.5 * delvc * (3.0 * pq_old - 4.0 * pq_half);
+        if (f_abs_lt(e_new, P.e_cut)) e_new = 0.0;
+        if (f_lt(e_new, P.emin)) e_new = P.emin;
+        p_new = pressure(bvcf, e_new, vnewc, P);
+        // corrector
+        double q_tilde;
+        if (f_gt(delvc, 0.)) q_tilde = 0.;
+        else q_tilde = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
+        e_new = e_new - (7.0 * pq_old - 8.0 * pq_half + (p_new + q_tilde)) * (delvc * (1.0 / 6.0));
+        if (f_abs_lt(e_new, P.e_cut)) e_new = 0.;
+        if (f_lt(e_new, P.emin)) e_new = P.emin;
+        p_new = pressure(bvcf, e_new, vnewc, P);
+        if (f_le(delvc, 0.)) {
+            q_new = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
+            if (f_abs_lt(q_new, P.q_cut)) q_new = 0.;
+        }
+    }
+    const double sst = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P));
+    m.ss[i] = sst;
+    m.p[i] = p_new;
+    m.e[i] = e_new;
+    m.q[i] = q_new;
+    return sst;
+}
+#endif
 
 __device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc, int rep) {
     return m.prm.refdens == 1.0 ? eos_body<true>(m, i, vnewc, rep) : eos_body<false>(m, i, vnewc, rep);
