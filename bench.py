@@ -368,7 +368,8 @@ def run_ours(args) -> None:
                                "host TimeIncrement per cycle",
                    "elements": ne, "nodes": nn, "mean_eos_rep": round(rep_avg, 3),
                    "parallelism": "replicas only (one independent problem per GPU)",
-                   "l2": f"no flush: working set {_working_set_gb(ne, nn):.1f} GB per GPU >> 129 MB L2"},
+                   "l2": f"no flush: working set {lul.Batch.footprint('fp64', args.size) / 1e9:.2f} GB "
+                         "per GPU >> 129 MB L2"},
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "how": "lulesh_leapfrog per cycle: upload step inputs from pinned host arrays, "
@@ -464,10 +465,6 @@ def run_serving(lul, n: int, seed: int, single_rate: float, budget_gb: float = 1
             "errors": sum(1 for x in results if x["err"] != 0), "gpu_launches": st["launches"],
             "how": "lulesh_serve: host worker builds each arrived Domain, the loop admits by HBM "
                    "footprint, replays ~20 ms graph chunks, retires at stoptime; wall clock"}
-
-
-def _working_set_gb(ne, nn) -> float:
-    return (13 * nn * 8 + nn + 13 * ne * 8 + 25 * ne * 4 + 48 * ne * 8 + 6 * ne * 8) / 1e9
 
 
 def run_reference(args) -> None:

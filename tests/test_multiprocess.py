@@ -1,0 +1,110 @@
+"""Multi-process host logic of bench.py on CPU (world size 2, gloo).
+
+bench.py runs one rank per GPU under torchrun: each rank solves its own
+problem (replicas, no data-path collective), the timed region is bracketed
+by a barrier, and rank 0 prints the max over ranks. The reference arm runs on
+rank 0 only. These tests exercise that host logic with CPU ranks; the GPU
+work of each rank is covered by the -m gpu tests.
+"""
+from __future__ import annotations
+
+import json
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _cpu_only():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("gloo rank test for machines without GPUs (bench picks nccl when CUDA is present)")
+
+
+def _rank_main(rank: int, world: int, port: int, out_dir: str) -> None:
+    os.environ.update(WORLD_SIZE=str(world), RANK=str(rank), LOCAL_RANK=str(rank),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, str(ROOT))
+    import torch.distributed as dist
+
+    import bench
+
+    r, w, local = bench.dist_init()
+    bench.barrier(w)
+    # each rank times a different duration; every rank must see the max
+    m = bench.max_over_ranks(1.5 + rank, w)
+    backend = dist.get_backend()
+    bench.barrier(w)
+    dist.destroy_process_group()
+    Path(out_dir, f"rank{rank}.json").write_text(
+        json.dumps({"rank": r, "world": w, "local": local, "max": m, "backend": backend}))
+
+
+def test_rank_setup_barrier_and_max_over_ranks(tmp_path):
+    _cpu_only()
+    import torch.multiprocessing as mp
+
+    mp.spawn(_rank_main, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
+    for rank in range(2):
+        d = json.loads((tmp_path / f"rank{rank}.json").read_text())
+        assert d == {"rank": rank, "world": 2, "local": rank, "max": 2.5, "backend": "gloo"}
+
+
+def test_reference_arm_prints_once_under_torchrun():
+    """The driver's own launch line with N=2: rank 0 times the reference's
+    CPU path and prints one JSON line; rank 1 exits 0 without work."""
+    _cpu_only()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), str(ROOT / "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--size", "8", "--steps", "2", "--warmup", "3"]
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["steps"] == 2 and d["warmup"] == 3
+    assert d["unit"] == "zone-cycles/s" and d["higher_is_better"] is True and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["elements"] == 8 ** 3
+
+
+def test_roofline_arithmetic():
+    """bench.roofline: dominant kernel, HBM fraction and the FP64-pipe roof
+    from the per-unit constants."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    ne, nn, cycles = 3_375_000, 3_442_951, 10
+    prof = {"kernel_ms": {"forces": 42.6, "nodes": 2.4, "kinematics": 20.6, "material": 14.7},
+            "cycles": cycles}
+    rl = bench.roofline(prof, "fp64", ne, nn, 3.26, fp64_peak=1.2, fp64_kind="test")
+    assert rl["kernel"] == "forces" and rl["bound"] == "hbm" and rl["unit"] == "GB/s"
+    launch_s = 42.6 / cycles / 1e3
+    assert rl["avg_launch_ms"] == pytest.approx(4.26)
+    assert rl["bytes_per_launch"] == bench.BYTES_PER_UNIT["fp64"]["forces"] * ne
+    assert rl["achieved"] == pytest.approx(rl["bytes_per_launch"] / launch_s / 1e9, rel=1e-3)
+    assert rl["frac"] == pytest.approx(rl["achieved"] / rl["peak"], rel=1e-3)
+    assert rl["traffic"] == bench.TRAFFIC_PER_UNIT["fp64"]["forces"] * ne
+    fp = rl["fp64_pipe"]
+    rate = bench.FP64_INSTR_PER_UNIT["fp64"]["forces"] * ne / launch_s
+    assert fp["achieved_ginst_s"] == pytest.approx(rate / 1e9, rel=1e-3)
+    assert fp["frac"] == pytest.approx(rate / 0.6e12, rel=1e-3)
+    assert sum(rl["kernel_share"].values()) == pytest.approx(1.0, abs=1e-3)
+    # the material kernel has no fixed instruction count: no pipe roof claimed
+    prof["kernel_ms"]["material"] = 99.0
+    assert bench.roofline(prof, "fp64", ne, nn, 3.26)["fp64_pipe"] is None
