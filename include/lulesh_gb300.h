@@ -87,6 +87,16 @@ typedef struct lulesh_domain_view {
     lulesh_time_state* time; /* may be NULL except for lulesh_leapfrog */
 } lulesh_domain_view;
 
+/* One Sedov problem of the reference's command line (--s --r --b --c), for the
+ * device build and the batch. */
+typedef struct lulesh_problem {
+    int32_t s, nr, balance, cost; /* --s --r --b --c */
+    double energy_scale;          /* deposited energy multiplier (1.0 = the reference) */
+    double stoptime;              /* <= 0: the reference's 1e-2 */
+    int32_t max_cycles;           /* <= 0: no cycle limit (the reference's --i default) */
+    int32_t pad_;
+} lulesh_problem;
+
 /* Field groups for lulesh_dev_upload / lulesh_dev_download. */
 #define LULESH_F_POS 0x001u   /* x y z */
 #define LULESH_F_VEL 0x002u   /* xd yd zd */
@@ -103,6 +113,11 @@ typedef struct lulesh_domain_view {
     (LULESH_F_POS | LULESH_F_VEL | LULESH_F_ACC | LULESH_F_FORCE | LULESH_F_EPQ |          \
      LULESH_F_V | LULESH_F_QLQQ | LULESH_F_KIN | LULESH_F_SS)
 #define LULESH_F_ALL 0x1ffu
+/* The constant mesh, download only: nodalMass volo elemMass nodelist
+ * lxim..lzetap elemBC nodeElemStart nodeElemCornerList (the upload calls
+ * refuse it with LULESH_EINVAL: the mesh is fixed when a handle or slot is
+ * created). */
+#define LULESH_F_MESH 0x200u
 
 typedef struct lulesh_dev lulesh_dev;
 typedef struct lulesh_domain lulesh_domain;
@@ -127,6 +142,16 @@ int lulesh_time_increment(lulesh_time_state* ts);
  * out[0] MaxAbsDiff, out[1] TotalAbsDiff, out[2] MaxRelDiff. */
 int lulesh_symmetry(const lulesh_domain_view* v, double out[3]);
 
+/* Final report of a run (VerifyAndWriteFinalOutput, lulesh-util.cc:60-115)
+ * as computed on the device by lulesh_dev_verify / lulesh_batch_verify:
+ * e(0) and the plane-0 symmetry diffs, bit for bit what lulesh_symmetry
+ * gives on the downloaded energy field. */
+typedef struct lulesh_verify_result {
+    double e0;                      /* final origin energy */
+    double maxabs, totabs, maxrel;  /* MaxAbsDiff, TotalAbsDiff, MaxRelDiff */
+    int32_t cycle, nx;              /* cycles run, problem edge s */
+} lulesh_verify_result;
+
 /* ---------------- device handle ------------------------------------------------------ */
 
 /* Allocates device mirrors of the Domain arrays the step touches and uploads
@@ -136,9 +161,24 @@ int lulesh_symmetry(const lulesh_domain_view* v, double out[3]);
 int lulesh_dev_create(const lulesh_domain_view* host, int32_t precision, lulesh_dev** out);
 void lulesh_dev_destroy(lulesh_dev* dev);
 
+/* Builds problem `p` (as Domain::Domain, lulesh-init.cc:10-183) directly in
+ * device memory: no host Domain and no upload. Every array equals the host
+ * build's bit for bit; the region sets are drawn on the host (the reference's
+ * rand() sequence) and expanded on the device. *ts receives the initial time
+ * state (with p->stoptime when > 0); pass it to lulesh_dev_run. Download
+ * fields into the view of a host Domain of the same problem when needed. */
+int lulesh_dev_create_problem(const lulesh_problem* p, int32_t precision, lulesh_time_state* ts,
+                              lulesh_dev** out);
+
 /* Copies field groups host -> device / device -> host (LULESH_F_* masks). */
 int lulesh_dev_upload(lulesh_dev* dev, const lulesh_domain_view* host, uint32_t mask);
 int lulesh_dev_download(lulesh_dev* dev, lulesh_domain_view* host, uint32_t mask);
+
+/* The final report of the device-resident state (e(0), plane-0 symmetry)
+ * without downloading any field; `cycle` is the caller's count of cycles run
+ * (copied into the result, as the reference prints it). Blocks until done.
+ * LULESH_EINVAL unless the mesh is a cube of edge nx (numElem = nx^3). */
+int lulesh_dev_verify(lulesh_dev* dev, int32_t cycle, lulesh_verify_result* out);
 
 /* One LagrangeLeapFrog cycle (lulesh.cc:1977-2240) on the device-resident
  * state with time step `deltatime`; returns the new Courant and hydro
@@ -173,14 +213,6 @@ int lulesh_dev_run_graph(lulesh_dev* dev, lulesh_time_state* ts, int32_t max_cyc
  * keeps its own dt, stoptime and cycle limit; problems join (admit) and
  * leave (retire) between graph replays without re-capturing the graph. */
 typedef struct lulesh_batch lulesh_batch;
-
-typedef struct lulesh_problem {
-    int32_t s, nr, balance, cost; /* --s --r --b --c */
-    double energy_scale;          /* deposited energy multiplier (1.0 = the reference) */
-    double stoptime;              /* <= 0: the reference's 1e-2 */
-    int32_t max_cycles;           /* <= 0: no cycle limit (the reference's --i default) */
-    int32_t pad_;
-} lulesh_problem;
 
 typedef struct lulesh_slot_status {
     int32_t in_use, active, cycle, err; /* err: 0 or LULESH_EVOLUME */
@@ -223,6 +255,8 @@ int lulesh_batch_run(lulesh_batch* b, int32_t cycles, int32_t* active_slots, dou
 int lulesh_batch_status(const lulesh_batch* b, lulesh_slot_status* out, int32_t n);
 /* Copies fields of one slot into a host view of the same problem size. */
 int lulesh_batch_download(lulesh_batch* b, int32_t slot, lulesh_domain_view* host, uint32_t mask);
+/* The final report of one slot, computed on the device (as lulesh_dev_verify). */
+int lulesh_batch_verify(lulesh_batch* b, int32_t slot, lulesh_verify_result* out);
 /* Times candidate launch shapes and tile sizes on the resident problems
  * (their state is saved first and restored after, so tuning does not
  * advance them), keeps the fastest and reports it. */
@@ -252,6 +286,7 @@ typedef struct lulesh_request_result {
     int32_t cycles, err, s, pad_;
     double arrival_s, admitted_s, finished_s, time_to_solution_s;
     double e0; /* final origin energy */
+    double maxabs, totabs, maxrel; /* plane-0 symmetry, computed on the device at retire */
     int64_t zone_cycles;
 } lulesh_request_result;
 

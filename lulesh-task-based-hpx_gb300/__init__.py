@@ -29,6 +29,7 @@ F_POS, F_VEL, F_ACC, F_FORCE, F_EPQ, F_V, F_QLQQ, F_KIN, F_SS = (1 << k for k in
 F_STEP_IN = F_POS | F_VEL | F_EPQ | F_V | F_SS
 F_STEP_OUT = F_POS | F_VEL | F_ACC | F_FORCE | F_EPQ | F_V | F_QLQQ | F_KIN | F_SS
 F_ALL = 0x1FF
+F_MESH = 0x200  # the constant mesh arrays, download only
 
 PHASE_FORCES, PHASE_NODES, PHASE_KINEMATICS, PHASE_MATERIAL = range(4)
 
@@ -90,7 +91,16 @@ class Request(C.Structure):
 class RequestResult(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("cycles", "err", "s", "pad_")] + \
                [(n, C.c_double) for n in ("arrival_s", "admitted_s", "finished_s", "time_to_solution_s",
-                                          "e0")] + [("zone_cycles", C.c_int64)]
+                                          "e0", "maxabs", "totabs", "maxrel")] + [("zone_cycles", C.c_int64)]
+
+
+class VerifyResult(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("e0", "maxabs", "totabs", "maxrel")] + \
+               [("cycle", C.c_int32), ("nx", C.c_int32)]
+
+
+def _verify_dict(r: VerifyResult) -> dict:
+    return {k: getattr(r, k) for k, _ in VerifyResult._fields_}
 
 
 class ServeStats(C.Structure):
@@ -134,8 +144,10 @@ def library() -> C.CDLL:
         "lulesh_symmetry": (i32, [C.POINTER(DomainView), C.POINTER(dbl)]),
         "lulesh_dev_create": (i32, [C.POINTER(DomainView), i32, C.POINTER(vp)]),
         "lulesh_dev_destroy": (None, [vp]),
+        "lulesh_dev_create_problem": (i32, [C.POINTER(Problem), i32, C.POINTER(TimeState), C.POINTER(vp)]),
         "lulesh_dev_upload": (i32, [vp, C.POINTER(DomainView), u32]),
         "lulesh_dev_download": (i32, [vp, C.POINTER(DomainView), u32]),
+        "lulesh_dev_verify": (i32, [vp, i32, C.POINTER(VerifyResult)]),
         "lulesh_dev_step": (i32, [vp, dbl, C.POINTER(dbl), C.POINTER(dbl)]),
         "lulesh_leapfrog": (i32, [vp, C.POINTER(DomainView)]),
         "lulesh_dev_run": (i32, [vp, C.POINTER(TimeState), i32, C.POINTER(i32)]),
@@ -158,6 +170,7 @@ def library() -> C.CDLL:
         "lulesh_batch_run": (i32, [vp, i32, C.POINTER(i32), C.POINTER(dbl)]),
         "lulesh_batch_status": (i32, [vp, C.POINTER(SlotStatus), i32]),
         "lulesh_batch_download": (i32, [vp, i32, C.POINTER(DomainView), u32]),
+        "lulesh_batch_verify": (i32, [vp, i32, C.POINTER(VerifyResult)]),
         "lulesh_batch_autotune": (i32, [vp, i32, C.POINTER(BatchTuning)]),
         "lulesh_batch_get_tuning": (i32, [vp, C.POINTER(BatchTuning)]),
         "lulesh_batch_set_tuning": (i32, [vp, C.POINTER(BatchTuning)]),
@@ -199,7 +212,8 @@ class HostDomain:
     Field arrays (numpy views onto the library's host vectors): the node fields
     x y z xd yd zd xdd ydd zdd fx fy fz nodalMass and the element fields
     e p q ql qq v vnew delv vdov arealg ss volo elemMass, plus the index
-    arrays nodelist nodeElemStart nodeElemCornerList regNumList.
+    arrays nodelist nodeElemStart nodeElemCornerList regNumList, the face
+    neighbours lxim lxip letam letap lzetam lzetap and elemBC.
     """
 
     def __init__(self, s: int, nr: int = 11, balance: int = 1, cost: int = 1,
@@ -226,6 +240,8 @@ class HostDomain:
         self.nodeElemStart = _np(v.nodeElemStart, v.numNode + 1, np.int32)
         self.nodeElemCornerList = _np(v.nodeElemCornerList, 8 * v.numElem, np.int32)
         self.regNumList = _np(v.regNumList, v.numElem, np.int32)
+        for f in ("lxim", "lxip", "letam", "letap", "lzetam", "lzetap", "elemBC"):
+            setattr(self, f, _np(getattr(v, f), v.numElem, np.int32))
         self.time_state = v.time.contents
 
     def symmetry(self) -> tuple[float, float, float]:
@@ -256,8 +272,42 @@ class HostDomain:
         self.close()
 
 
+class DeviceBuilt:
+    """Time state of a problem built on the device (Device.from_problem): it
+    has no host arrays; download into the view of a HostDomain of the same
+    problem when fields are needed."""
+
+    view_ptr = None
+
+    def __init__(self, s: int):
+        self.s = s
+        self.time_state = TimeState()
+
+    @property
+    def cycle(self) -> int:
+        return self.time_state.cycle
+
+
 class Device:
     """Device mirror of a HostDomain; every method runs the sm_103a kernels."""
+
+    @classmethod
+    def from_problem(cls, s: int, nr: int = 11, balance: int = 1, cost: int = 1,
+                     energy_scale: float = 1.0, precision: str = "fp64", stoptime: float = 0.0) -> "Device":
+        """Builds the problem directly in device memory (lulesh_dev_create_problem):
+        no host Domain is built and nothing but the region runs is uploaded."""
+        lib = library()
+        self = cls.__new__(cls)
+        state = DeviceBuilt(s)
+        prob = Problem(s, nr, balance, cost, energy_scale, stoptime, 0, 0)
+        h = C.c_void_p()
+        _check(lib.lulesh_dev_create_problem(C.byref(prob), PRECISION[precision], C.byref(state.time_state),
+                                             C.byref(h)), "lulesh_dev_create_problem")
+        self._h = h
+        self._lib = lib
+        self.dom = state
+        self.precision = precision
+        return self
 
     def __init__(self, dom: HostDomain, precision: str = "fp64"):
         lib = library()
@@ -272,8 +322,21 @@ class Device:
     def upload(self, mask: int = F_ALL) -> None:
         _check(self._lib.lulesh_dev_upload(self._h, self.dom.view_ptr, mask), "lulesh_dev_upload")
 
-    def download(self, mask: int = F_ALL) -> None:
-        _check(self._lib.lulesh_dev_download(self._h, self.dom.view_ptr, mask), "lulesh_dev_download")
+    def download(self, mask: int = F_ALL, into: "HostDomain | None" = None) -> None:
+        """Device fields -> the host view of self.dom, or of `into` (a HostDomain
+        of the same problem; needed for a device-built problem)."""
+        target = self.dom if into is None else into
+        if target.view_ptr is None:
+            raise ValueError("a device-built problem has no host arrays: pass into=HostDomain(...)")
+        _check(self._lib.lulesh_dev_download(self._h, target.view_ptr, mask), "lulesh_dev_download")
+
+    def verify(self) -> dict:
+        """Final report computed on the device (lulesh_dev_verify): e0,
+        maxabs, totabs, maxrel, cycle, nx; no field is downloaded."""
+        r = VerifyResult()
+        _check(self._lib.lulesh_dev_verify(self._h, self.dom.time_state.cycle, C.byref(r)),
+               "lulesh_dev_verify")
+        return _verify_dict(r)
 
     def step(self, dt: float) -> tuple[float, float]:
         dtc, dth = C.c_double(), C.c_double()
@@ -449,6 +512,12 @@ class Batch:
         dom = HostDomain(sp["s"], sp["nr"], sp["balance"], sp["cost"], sp["energy_scale"])
         _check(self._lib.lulesh_batch_download(self._h, slot, dom.view_ptr, mask), "lulesh_batch_download")
         return dom
+
+    def verify(self, slot: int) -> dict:
+        """Final report of a slot computed on the device (lulesh_batch_verify)."""
+        r = VerifyResult()
+        _check(self._lib.lulesh_batch_verify(self._h, slot, C.byref(r)), "lulesh_batch_verify")
+        return _verify_dict(r)
 
     def autotune(self, cycles: int = 2) -> dict:
         t = BatchTuning()

@@ -5,9 +5,10 @@ parallel), links liblulesh_gb300.so next to this file and the lulesh-gb300
 executable (the reference's command line on top of the C ABI).
 
 Floating-point contraction is part of the numerics contract:
-  * fp64_exact.cu and time_increment.cu are built with --fmad=false, so the
-    exact double path and the device TimeIncrement round every operation
-    separately, as the reference source is written;
+  * fp64_exact.cu, time_increment.cu, verify.cu and device_init.cu are
+    built with --fmad=false, so the exact double path, the device
+    TimeIncrement, the device final report and the device problem build
+    round every operation separately, as the reference source is written;
   * domain.cpp (problem set-up, host TimeIncrement) is built with
     -ffp-contract=off so the host numbers do not depend on whether the host
     compiler fuses multiply-adds (GCC does by default on aarch64).
@@ -38,6 +39,8 @@ UNITS = [
     ("fp64_exact.cu", ["--fmad=false"]),
     ("mixed.cu", []),
     ("time_increment.cu", ["--fmad=false"]),
+    ("verify.cu", ["--fmad=false"]),
+    ("device_init.cu", ["--fmad=false"]),
     ("capi.cu", []),
     ("noalloc.cu", []),
     ("probe.cu", []),

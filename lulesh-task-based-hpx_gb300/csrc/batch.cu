@@ -108,12 +108,6 @@ Launch3 batch_launchers(int precision) {
     }
 }
 
-int rep_of(int reg, int numReg, int cost) {  // lulesh.cc:2156-2170
-    if (reg < numReg / 2) return 1;
-    if (reg < (numReg - (numReg + 15) / 20)) return 1 + cost;
-    return 10 * (1 + cost);
-}
-
 }  // namespace
 
 struct lulesh_batch {
@@ -132,11 +126,13 @@ struct lulesh_batch {
     size_t tile_cap[3] = {0, 0, 0};
     int32_t* d_ntiles = nullptr;
     unsigned* d_queue = nullptr;
+    double* d_verify = nullptr;  // [4] lulesh_batch_verify output
     // pinned host mirrors
     Mesh* h_meshes = nullptr;
     DevTime* h_times = nullptr;
     StepResult* h_results = nullptr;
     int32_t* h_ntiles = nullptr;
+    double* h_verify = nullptr;
     std::vector<BatchTile> h_tiles[3];
     // launch shapes and graph
     Launch3 L{};
@@ -149,6 +145,70 @@ struct lulesh_batch {
 };
 
 namespace {
+
+int free_slot(const lulesh_batch* b) {
+    for (int i = 0; i < int(b->slots.size()); ++i)
+        if (!b->slots[i].in_use) return i;
+    return -1;
+}
+
+// Completes an admission: the slot's mesh descriptor, time state (with its
+// own stoptime and cycle limit) and result word go to the device, and the
+// slot records its pool block and repeat classes (repeat count, elements).
+int finish_admit(lulesh_batch* b, int slot, size_t off, size_t bytes, Mesh m, const lulesh_time_state& ts,
+                 double stoptime, int32_t max_cycles, const std::vector<int2>& classes, int s,
+                 int32_t* slot_out) {
+    m.result = b->d_results + slot;
+    m.dtime = b->d_times + slot;
+    m.partials = nullptr;
+    m.matGrid = 0;
+    DevTime t{};
+    t.time = ts.time;
+    t.deltatime = ts.deltatime;
+    t.dtcourant = ts.dtcourant;
+    t.dthydro = ts.dthydro;
+    t.dtfixed = ts.dtfixed;
+    t.deltatimemultlb = ts.deltatimemultlb;
+    t.deltatimemultub = ts.deltatimemultub;
+    t.dtmax = ts.dtmax;
+    t.stoptime = stoptime > 0.0 ? stoptime : ts.stoptime;
+    t.cycle = ts.cycle;
+    t.max_cycles = max_cycles > 0 ? max_cycles : INT32_MAX;
+    t.active = 1;
+    StepResult r{};
+    r.dtcourant = r.dthydro = 1.0e+20;
+    Slot& sl = b->slots[slot];
+    sl.repCount.clear();
+    sl.repValue.clear();
+    for (const int2& c : classes) {
+        sl.repValue.push_back(c.x);
+        sl.repCount.push_back(c.y);
+    }
+    b->h_meshes[slot] = m;
+    b->h_times[slot] = t;
+    b->h_results[slot] = r;
+    auto release = [&](int code) {
+        b->pool.release(off, bytes);
+        return code;
+    };
+    if (cudaMemcpyAsync(b->d_meshes + slot, b->h_meshes + slot, sizeof(Mesh), cudaMemcpyHostToDevice, b->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(b->d_times + slot, b->h_times + slot, sizeof(DevTime), cudaMemcpyHostToDevice, b->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(b->d_results + slot, b->h_results + slot, sizeof(StepResult), cudaMemcpyHostToDevice,
+                        b->stream) != cudaSuccess ||
+        cudaStreamSynchronize(b->stream) != cudaSuccess)
+        return release(LULESH_ECUDA);
+    sl.in_use = true;
+    sl.off = off;
+    sl.bytes = bytes;
+    sl.s = s;
+    sl.numElem = m.numElem;
+    sl.numNode = m.numNode;
+    b->tiles_dirty = true;
+    if (slot_out) *slot_out = slot;
+    return LULESH_OK;
+}
 
 BatchCtl make_ctl(const lulesh_batch* b) {
     BatchCtl c{};
@@ -305,9 +365,10 @@ void lulesh_batch_destroy(lulesh_batch* b) {
     if (b->ev1) cudaEventDestroy(b->ev1);
     for (void* p : {(void*)b->pool_base, (void*)b->d_meshes, (void*)b->d_times, (void*)b->d_results,
                     (void*)b->d_tiles[0], (void*)b->d_tiles[1], (void*)b->d_tiles[2],
-                    (void*)b->d_ntiles, (void*)b->d_queue})
+                    (void*)b->d_ntiles, (void*)b->d_queue, (void*)b->d_verify})
         if (p) cudaFree(p);
-    for (void* p : {(void*)b->h_meshes, (void*)b->h_times, (void*)b->h_results, (void*)b->h_ntiles})
+    for (void* p : {(void*)b->h_meshes, (void*)b->h_times, (void*)b->h_results, (void*)b->h_ntiles,
+                    (void*)b->h_verify})
         if (p) cudaFreeHost(p);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -342,12 +403,14 @@ int lulesh_batch_create(int32_t precision, uint64_t pool_bytes, int32_t max_slot
         cudaMalloc(&b->d_times, n * sizeof(DevTime)) != cudaSuccess ||
         cudaMalloc(&b->d_results, n * sizeof(StepResult)) != cudaSuccess ||
         cudaMalloc(&b->d_ntiles, 3 * sizeof(int32_t)) != cudaSuccess ||
-        cudaMalloc(&b->d_queue, 4 * sizeof(unsigned)) != cudaSuccess)
+        cudaMalloc(&b->d_queue, 4 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&b->d_verify, 4 * sizeof(double)) != cudaSuccess)
         return fail(LULESH_ENOMEM);
     if (cudaMallocHost(&b->h_meshes, n * sizeof(Mesh)) != cudaSuccess ||
         cudaMallocHost(&b->h_times, n * sizeof(DevTime)) != cudaSuccess ||
         cudaMallocHost(&b->h_results, n * sizeof(StepResult)) != cudaSuccess ||
-        cudaMallocHost(&b->h_ntiles, 3 * sizeof(int32_t)) != cudaSuccess)
+        cudaMallocHost(&b->h_ntiles, 3 * sizeof(int32_t)) != cudaSuccess ||
+        cudaMallocHost(&b->h_verify, 4 * sizeof(double)) != cudaSuccess)
         return fail(LULESH_ENOMEM);
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
@@ -378,20 +441,26 @@ int lulesh_batch_create(int32_t precision, uint64_t pool_bytes, int32_t max_slot
 }
 
 int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot_out) {
-    if (!b || !p) return LULESH_EINVAL;
-    if (p->s < 1 || p->s > 640 || p->nr < 1 || p->balance < 0 || p->cost < 0 || !(p->energy_scale > 0.0))
-        return LULESH_EINVAL;
-    // refuse before the host set-up when the problem cannot fit
-    bool free_slot = false;
-    for (const Slot& sl : b->slots) free_slot |= !sl.in_use;
+    if (!b) return LULESH_EINVAL;
+    int st = lulesh::check_problem(p);
+    if (st != LULESH_OK) return st;
+    const int slot = free_slot(b);
+    if (slot < 0) return LULESH_ENOMEM;
     const int ne = p->s * p->s * p->s, nn = (p->s + 1) * (p->s + 1) * (p->s + 1);
-    if (!free_slot || b->pool.largest_free() < lulesh::mesh_bytes(b->precision, ne, nn)) return LULESH_ENOMEM;
-    lulesh_domain* hd = nullptr;
-    int st = lulesh_domain_create(p->s, p->nr, p->balance, p->cost, p->energy_scale, &hd);
-    if (st == LULESH_OK)
-        st = lulesh_batch_admit_view(b, lulesh_domain_get_view(hd), p->stoptime, p->max_cycles, slot_out);
-    lulesh_domain_destroy(hd);
-    return st;
+    const size_t bytes = lulesh::mesh_bytes(b->precision, ne, nn);
+    const size_t off = b->pool.alloc(bytes);
+    if (off == SIZE_MAX) return LULESH_ENOMEM;
+    // built on the device: no host Domain, nothing uploaded but the region runs
+    Mesh m{};
+    lulesh_time_state ts{};
+    std::vector<int2> classes;
+    st = lulesh::mesh_init_problem(m, b->pool_base + off, p, b->precision, b->stream, &ts, &classes);
+    if (st != LULESH_OK) {
+        b->pool.release(off, bytes);
+        return st;
+    }
+    b->launches += b->precision == LULESH_MIXED ? 5 : 4;
+    return finish_admit(b, slot, off, bytes, m, ts, p->stoptime, p->max_cycles, classes, p->s, slot_out);
 }
 
 int lulesh_batch_admit_view(lulesh_batch* b, const lulesh_domain_view* v, double stoptime,
@@ -399,12 +468,7 @@ int lulesh_batch_admit_view(lulesh_batch* b, const lulesh_domain_view* v, double
     if (!b || !v || !v->time) return LULESH_EINVAL;
     int st = lulesh::validate_view(v);
     if (st != LULESH_OK) return st;
-    int slot = -1;
-    for (int i = 0; i < int(b->slots.size()); ++i)
-        if (!b->slots[i].in_use) {
-            slot = i;
-            break;
-        }
+    const int slot = free_slot(b);
     if (slot < 0) return LULESH_ENOMEM;
     const int ne = v->numElem, nn = v->numNode;
     const size_t bytes = lulesh::mesh_bytes(b->precision, ne, nn);
@@ -416,58 +480,35 @@ int lulesh_batch_admit_view(lulesh_batch* b, const lulesh_domain_view* v, double
         b->pool.release(off, bytes);
         return st;
     }
-    m.result = b->d_results + slot;
-    m.dtime = b->d_times + slot;
-    m.partials = nullptr;
-    m.matGrid = 0;
-    DevTime t{};
-    const lulesh_time_state* ts = v->time;
-    t.time = ts->time;
-    t.deltatime = ts->deltatime;
-    t.dtcourant = ts->dtcourant;
-    t.dthydro = ts->dthydro;
-    t.dtfixed = ts->dtfixed;
-    t.deltatimemultlb = ts->deltatimemultlb;
-    t.deltatimemultub = ts->deltatimemultub;
-    t.dtmax = ts->dtmax;
-    t.stoptime = stoptime > 0.0 ? stoptime : ts->stoptime;
-    t.cycle = ts->cycle;
-    t.max_cycles = max_cycles > 0 ? max_cycles : INT32_MAX;
-    t.active = 1;
-    StepResult r{};
-    r.dtcourant = r.dthydro = 1.0e+20;
     // repeat classes in matOrder order (largest repeat count first)
-    Slot& sl = b->slots[slot];
-    std::map<int, int, std::greater<int>> classes;
-    for (int i = 0; i < ne; ++i) ++classes[rep_of(v->regNumList[i] - 1, v->numReg, v->cost)];
-    sl.repCount.clear();
-    sl.repValue.clear();
-    for (const auto& kv : classes) {
-        sl.repValue.push_back(kv.first);
-        sl.repCount.push_back(kv.second);
-    }
-    b->h_meshes[slot] = m;
-    b->h_times[slot] = t;
-    b->h_results[slot] = r;
-    BCK(cudaMemcpyAsync(b->d_meshes + slot, b->h_meshes + slot, sizeof(Mesh), cudaMemcpyHostToDevice, b->stream));
-    BCK(cudaMemcpyAsync(b->d_times + slot, b->h_times + slot, sizeof(DevTime), cudaMemcpyHostToDevice, b->stream));
-    BCK(cudaMemcpyAsync(b->d_results + slot, b->h_results + slot, sizeof(StepResult), cudaMemcpyHostToDevice, b->stream));
-    BCK(cudaStreamSynchronize(b->stream));
-    sl.in_use = true;
-    sl.off = off;
-    sl.bytes = bytes;
-    sl.s = v->sizeX;
-    sl.numElem = ne;
-    sl.numNode = nn;
-    b->tiles_dirty = true;
-    if (slot_out) *slot_out = slot;
-    return LULESH_OK;
+    std::map<int, int, std::greater<int>> count;
+    for (int i = 0; i < ne; ++i) ++count[lulesh::region_rep(v->regNumList[i] - 1, v->numReg, v->cost)];
+    std::vector<int2> classes;
+    for (const auto& kv : count) classes.push_back(make_int2(kv.first, kv.second));
+    return finish_admit(b, slot, off, bytes, m, *v->time, stoptime, max_cycles, classes, v->sizeX, slot_out);
 }
 
 int lulesh_batch_origin_energy(lulesh_batch* b, int32_t slot, double* e0) {
     if (!b || !e0 || slot < 0 || slot >= int(b->slots.size()) || !b->slots[slot].in_use) return LULESH_EINVAL;
     BCK(cudaMemcpyAsync(e0, b->h_meshes[slot].e, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
+    return LULESH_OK;
+}
+
+int lulesh_batch_verify(lulesh_batch* b, int32_t slot, lulesh_verify_result* out) {
+    if (!b || !out || slot < 0 || slot >= int(b->slots.size()) || !b->slots[slot].in_use) return LULESH_EINVAL;
+    const Slot& sl = b->slots[slot];
+    if (sl.s < 1 || int64_t(sl.s) * sl.s * sl.s != int64_t(sl.numElem)) return LULESH_EINVAL;
+    b->launches += lulesh::launch_verify(b->h_meshes[slot].e, sl.s, b->d_verify, b->stream);
+    BCK(cudaGetLastError());
+    BCK(cudaMemcpyAsync(b->h_verify, b->d_verify, 4 * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    out->e0 = b->h_verify[0];
+    out->maxabs = b->h_verify[1];
+    out->totabs = b->h_verify[2];
+    out->maxrel = b->h_verify[3];
+    out->cycle = b->h_times[slot].cycle;
+    out->nx = sl.s;
     return LULESH_OK;
 }
 

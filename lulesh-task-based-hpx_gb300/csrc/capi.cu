@@ -38,13 +38,6 @@ Launchers launchers_for(int precision) {
     }
 }
 
-// Number of EOS evaluations of region index reg (0-based) (lulesh.cc:2156-2170).
-int region_rep(int reg, int numReg, int cost) {
-    if (reg < numReg / 2) return 1;
-    if (reg < (numReg - (numReg + 15) / 20)) return 1 + cost;
-    return 10 * (1 + cost);
-}
-
 // Carves typed arrays out of one device allocation (256-byte aligned).
 struct Arena {
     size_t used = 0;
@@ -73,6 +66,9 @@ struct lulesh_dev {
     int graph_kernels = 0;
     int64_t launches = 0;
     int32_t err_elem = -1;
+    int32_t nx = 0;                  // edge of the cube (Domain::sizeX)
+    double* d_verify = nullptr;      // [4] lulesh_dev_verify output (arena)
+    double* h_verify = nullptr;      // [4] pinned
     Launchers L{};
     // device-side timing (lulesh_dev_profile_begin/end)
     bool profiling = false;
@@ -173,6 +169,7 @@ void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     m.partials = a.take<lulesh::DtPartial>(matGrid);
     m.result = a.take<StepResult>(1);
     d->d_time = a.take<DevTime>(1);
+    d->d_verify = a.take<double>(4);
 }
 
 struct Copy {
@@ -198,6 +195,23 @@ std::vector<Copy> groups(const Mesh& m, const lulesh_domain_view* v, uint32_t ma
         c.insert(c.end(), {{m.vnew, v->vnew, eb}, {m.delv, v->delv, eb}, {m.vdov, v->vdov, eb},
                            {m.arealg, v->arealg, eb}});
     if (mask & LULESH_F_SS) c.push_back({m.ss, v->ss, eb});
+    if (mask & LULESH_F_MESH) {
+        const size_t ib = sizeof(int32_t) * size_t(m.numElem);
+        c.insert(c.end(), {{const_cast<double*>(m.nodalMass), v->nodalMass, nb},
+                           {const_cast<double*>(m.volo), v->volo, eb},
+                           {const_cast<double*>(m.elemMass), v->elemMass, eb},
+                           {const_cast<int32_t*>(m.nodelist), v->nodelist, 8 * ib},
+                           {const_cast<int32_t*>(m.lxim), v->lxim, ib},
+                           {const_cast<int32_t*>(m.lxip), v->lxip, ib},
+                           {const_cast<int32_t*>(m.letam), v->letam, ib},
+                           {const_cast<int32_t*>(m.letap), v->letap, ib},
+                           {const_cast<int32_t*>(m.lzetam), v->lzetam, ib},
+                           {const_cast<int32_t*>(m.lzetap), v->lzetap, ib},
+                           {const_cast<int32_t*>(m.elemBC), v->elemBC, ib},
+                           {const_cast<int32_t*>(m.nodeElemStart), v->nodeElemStart,
+                            sizeof(int32_t) * (size_t(m.numNode) + 1)},
+                           {const_cast<int32_t*>(m.nodeElemCornerList), v->nodeElemCornerList, 8 * ib}});
+    }
     return c;
 }
 
@@ -216,7 +230,7 @@ int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaS
     std::vector<double> invMass(nn);
     for (int k = 0; k < nn; ++k) invMass[k] = 1.0 / v->nodalMass[k];
     std::vector<int32_t> rep(ne), order(ne);
-    for (int i = 0; i < ne; ++i) rep[i] = region_rep(v->regNumList[i] - 1, v->numReg, v->cost);
+    for (int i = 0; i < ne; ++i) rep[i] = lulesh::region_rep(v->regNumList[i] - 1, v->numReg, v->cost);
     for (int i = 0; i < ne; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rep[a] > rep[b]; });
 
@@ -307,24 +321,17 @@ int build_graph(lulesh_dev* d) {
     return LULESH_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev** out) {
-    if (!out) return LULESH_EINVAL;
-    *out = nullptr;
+// A handle for ne elements and nn nodes: the arena carved, the stream and
+// the pinned result buffers created, the device result word cleared. The
+// mesh arrays are left for the caller to fill.
+int new_handle(int32_t precision, int ne, int nn, lulesh_dev** out) {
     if (precision != LULESH_FP64 && precision != LULESH_FP64_EXACT && precision != LULESH_MIXED)
         return LULESH_EINVAL;
-    int st = check_view(v);
-    if (st != LULESH_OK) return st;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LULESH_ENODEV;
     int dev_id = 0, sms = 0;
     CK(cudaGetDevice(&dev_id));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
-
-    const int ne = v->numElem, nn = v->numNode;
     lulesh_dev* d = new (std::nothrow) lulesh_dev;
     if (!d) return LULESH_ENOMEM;
     d->precision = precision;
@@ -345,18 +352,59 @@ int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev
     m.numElem = ne;
     m.numNode = nn;
     m.matGrid = matGrid;
-    m.prm = v->params;
     m.dtime = nullptr;
     if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(LULESH_ECUDA);
     if (cudaMallocHost(&d->h_result, sizeof(StepResult)) != cudaSuccess) return fail(LULESH_ENOMEM);
     if (cudaMallocHost(&d->h_time, sizeof(DevTime)) != cudaSuccess) return fail(LULESH_ENOMEM);
-
+    if (cudaMallocHost(&d->h_verify, 4 * sizeof(double)) != cudaSuccess) return fail(LULESH_ENOMEM);
     if (cudaMemsetAsync(m.result, 0, sizeof(StepResult), d->stream) != cudaSuccess)
         return fail(LULESH_ECUDA);
-    st = upload_mesh(m, v, precision, d->stream);
-    if (st != LULESH_OK) return fail(st);
+    *out = d;
+    return LULESH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev** out) {
+    if (!out) return LULESH_EINVAL;
+    *out = nullptr;
+    int st = check_view(v);
+    if (st != LULESH_OK) return st;
+    lulesh_dev* d = nullptr;
+    st = new_handle(precision, v->numElem, v->numNode, &d);
+    if (st != LULESH_OK) return st;
+    d->m.prm = v->params;
+    d->nx = v->sizeX;
+    st = upload_mesh(d->m, v, precision, d->stream);
+    if (st != LULESH_OK) {
+        lulesh_dev_destroy(d);
+        return st;
+    }
     if (precision == LULESH_MIXED) ++d->launches;  // the float-pair mirror kernel
+    *out = d;
+    return LULESH_OK;
+}
+
+int lulesh_dev_create_problem(const lulesh_problem* p, int32_t precision, lulesh_time_state* ts,
+                              lulesh_dev** out) {
+    if (!out || !ts) return LULESH_EINVAL;
+    *out = nullptr;
+    int st = lulesh::check_problem(p);
+    if (st != LULESH_OK) return st;
+    const int ne = p->s * p->s * p->s, nn = (p->s + 1) * (p->s + 1) * (p->s + 1);
+    lulesh_dev* d = nullptr;
+    st = new_handle(precision, ne, nn, &d);
+    if (st != LULESH_OK) return st;
+    d->nx = p->s;
+    st = lulesh::mesh_fill_problem(d->m, p, precision, d->stream, ts, nullptr);
+    if (st != LULESH_OK) {
+        lulesh_dev_destroy(d);
+        return st;
+    }
+    d->launches += precision == LULESH_MIXED ? 5 : 4;  // the build kernels (and the mirror)
     *out = d;
     return LULESH_OK;
 }
@@ -372,12 +420,31 @@ void lulesh_dev_destroy(lulesh_dev* d) {
     if (d->arena) cudaFree(d->arena);
     if (d->h_result) cudaFreeHost(d->h_result);
     if (d->h_time) cudaFreeHost(d->h_time);
+    if (d->h_verify) cudaFreeHost(d->h_verify);
     if (d->stream) cudaStreamDestroy(d->stream);
     delete d;
 }
 
+int lulesh_dev_verify(lulesh_dev* d, int32_t cycle, lulesh_verify_result* out) {
+    if (!d || !out) return LULESH_EINVAL;
+    const int nx = d->nx;
+    if (nx < 1 || int64_t(nx) * nx * nx != int64_t(d->m.numElem)) return LULESH_EINVAL;
+    d->launches += lulesh::launch_verify(d->m.e, nx, d->d_verify, d->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(d->h_verify, d->d_verify, 4 * sizeof(double), cudaMemcpyDeviceToHost, d->stream));
+    CK(cudaStreamSynchronize(d->stream));
+    out->e0 = d->h_verify[0];
+    out->maxabs = d->h_verify[1];
+    out->totabs = d->h_verify[2];
+    out->maxrel = d->h_verify[3];
+    out->cycle = cycle;
+    out->nx = nx;
+    return LULESH_OK;
+}
+
 int lulesh_dev_upload(lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask) {
     if (!d || !v || v->numElem != d->m.numElem || v->numNode != d->m.numNode) return LULESH_EINVAL;
+    if (mask & LULESH_F_MESH) return LULESH_EINVAL;  // the mesh is fixed at creation
     for (const Copy& c : groups(d->m, v, mask)) {
         if (!c.host) return LULESH_EINVAL;
         CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, d->stream));
@@ -609,7 +676,84 @@ int mesh_init(Mesh& m, char* base, const lulesh_domain_view* v, int precision, c
     return upload_mesh(m, v, precision, s);
 }
 
+int check_problem(const lulesh_problem* p) {
+    if (!p) return LULESH_EINVAL;
+    // s^3 elements and 8 s^3 corner indices must fit the int32 indices
+    if (p->s < 1 || p->s > 640 || p->nr < 1 || p->balance < 0 || p->cost < 0 || !(p->energy_scale > 0.0))
+        return LULESH_EINVAL;
+    return LULESH_OK;
+}
+
+int mesh_fill_problem(Mesh& m, const lulesh_problem* p, int precision, cudaStream_t s, lulesh_time_state* ts,
+                      std::vector<int2>* classes) {
+    const int ne = m.numElem;
+    default_params(m.prm);
+    double einit = 0.0;
+    initial_time_state(p->s, p->energy_scale, *ts, einit);
+    if (p->stoptime > 0.0) ts->stoptime = p->stoptime;
+    // region runs in element order, and the same runs ordered by repeat
+    // count (largest first, element order within a count): the material
+    // phase's matOrder as (first, count) ranges
+    std::vector<RegionRun> runs;
+    region_runs(ne, p->nr, p->balance, runs);
+    const int nruns = int(runs.size());
+    std::vector<int> rep(nruns), idx(nruns);
+    for (int r = 0; r < nruns; ++r) {
+        rep[r] = region_rep(runs[r].reg - 1, p->nr, p->cost);
+        idx[r] = r;
+    }
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return rep[a] > rep[b]; });
+    std::vector<int2> order(nruns);
+    std::vector<int32_t> off(nruns + 1, 0);
+    for (int k = 0; k < nruns; ++k) {
+        order[k] = make_int2(runs[idx[k]].first, runs[idx[k]].count);
+        off[k + 1] = off[k] + runs[idx[k]].count;
+    }
+    if (classes) {
+        classes->clear();
+        for (int k = 0; k < nruns; ++k) {
+            const int r = rep[idx[k]];
+            if (classes->empty() || classes->back().x != r) classes->push_back(make_int2(r, 0));
+            classes->back().y += runs[idx[k]].count;
+        }
+    }
+    // the three tables in one stream-ordered temporary allocation
+    const size_t b_runs = (sizeof(RegionRun) * nruns + 255) & ~size_t(255);
+    const size_t b_order = (sizeof(int2) * nruns + 255) & ~size_t(255);
+    const size_t b_off = sizeof(int32_t) * (nruns + 1);
+    char* tab = nullptr;
+    CK(cudaMallocAsync(reinterpret_cast<void**>(&tab), b_runs + b_order + b_off, s));
+    RegionRun* d_runs = reinterpret_cast<RegionRun*>(tab);
+    int2* d_order = reinterpret_cast<int2*>(tab + b_runs);
+    int32_t* d_off = reinterpret_cast<int32_t*>(tab + b_runs + b_order);
+    int st = LULESH_OK;
+    if (cudaMemcpyAsync(d_runs, runs.data(), sizeof(RegionRun) * nruns, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d_order, order.data(), sizeof(int2) * nruns, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(d_off, off.data(), b_off, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        st = LULESH_ECUDA;
+    if (st == LULESH_OK) {
+        launch_build(m, p->s, einit, d_runs, nruns, d_order, d_off, nruns, p->nr, p->cost, s);
+        if (precision == LULESH_MIXED) mixed::launch_mirror(m, s);
+        if (cudaGetLastError() != cudaSuccess) st = LULESH_ECUDA;
+    }
+    cudaFreeAsync(tab, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) st = LULESH_ECUDA;
+    return st;
+}
+
+int mesh_init_problem(Mesh& m, char* base, const lulesh_problem* p, int precision, cudaStream_t s,
+                      lulesh_time_state* ts, std::vector<int2>* classes) {
+    Arena a;
+    a.base = base;
+    const int ne = p->s * p->s * p->s, nn = (p->s + 1) * (p->s + 1) * (p->s + 1);
+    carve_mesh(m, a, precision, ne, nn);
+    m.numElem = ne;
+    m.numNode = nn;
+    return mesh_fill_problem(m, p, precision, s, ts, classes);
+}
+
 int copy_fields(const Mesh& m, const lulesh_domain_view* v, uint32_t mask, bool to_device, cudaStream_t s) {
+    if (to_device && (mask & LULESH_F_MESH)) return LULESH_EINVAL;  // the mesh is fixed at admission
     for (const Copy& c : groups(m, v, mask)) {
         if (!c.host) return LULESH_EINVAL;
         if (to_device) CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, s));

@@ -109,10 +109,11 @@ void HostDomain::corner_csr() {
         }
 }
 
-void HostDomain::regions() {
+void region_runs(int numElem, int numReg, int balance, std::vector<RegionRun>& runs) {
+    runs.clear();
     srand(0);
     if (numReg == 1) {
-        std::fill(regNumList.begin(), regNumList.end(), 1);
+        runs.push_back({0, numElem, 1});
         return;
     }
     std::vector<int> binEnd(numReg);
@@ -140,10 +141,66 @@ void HostDomain::regions() {
         else if (bin < 978) run = rand() % 128 + 128;
         else if (bin < 981) run = rand() % 256 + 256;
         else run = rand() % 1537 + 512;
-        const int end = next + run;
-        while (next < end && next < numElem) regNumList[next++] = reg;
+        const int count = std::min(run, numElem - next);
+        runs.push_back({next, count, reg});
+        next += count;
         last = reg;
     }
+}
+
+void default_params(lulesh_params& P) {
+    P = lulesh_params{};
+    P.e_cut = 1.0e-7;
+    P.p_cut = 1.0e-7;
+    P.q_cut = 1.0e-7;
+    P.v_cut = 1.0e-10;
+    P.u_cut = 1.0e-7;
+    P.hgcoef = 3.0;
+    P.ss4o3 = 4.0 / 3.0;
+    P.qstop = 1.0e+12;
+    P.monoq_max_slope = 1.0;
+    P.monoq_limiter_mult = 2.0;
+    P.qlc_monoq = 0.5;
+    P.qqc_monoq = 2.0 / 3.0;
+    P.qqc = 2.0;
+    P.eosvmax = 1.0e+9;
+    P.eosvmin = 1.0e-9;
+    P.pmin = 0.0;
+    P.emin = -1.0e+15;
+    P.dvovmax = 0.1;
+    P.refdens = 1.0;
+}
+
+void initial_time_state(int s, double energy_scale, lulesh_time_state& ts, double& einit) {
+    ts = lulesh_time_state{};
+    ts.dtfixed = -1.0e-6;
+    ts.stoptime = 1.0e-2;
+    ts.deltatimemultlb = 1.1;
+    ts.deltatimemultub = 1.2;
+    ts.dtcourant = 1.0e+20;
+    ts.dthydro = 1.0e+20;
+    ts.dtmax = 1.0e-2;
+    ts.time = 0.0;
+    ts.cycle = 0;
+    const double ebase = 3.948746e+7;
+    const double scale = s / 45.0;
+    einit = ebase * scale * scale * scale;
+    if (energy_scale != 1.0) einit = einit * energy_scale;
+    // element 0's volume from its corner coordinates (as mesh() places them)
+    double xl[8], yl[8], zl[8];
+    const int dc[8] = {0, 1, 1, 0, 0, 1, 1, 0}, dr[8] = {0, 0, 1, 1, 0, 0, 1, 1};
+    for (int k = 0; k < 8; ++k) {
+        xl[k] = 1.125 * double(dc[k]) / double(s);
+        yl[k] = 1.125 * double(dr[k]) / double(s);
+        zl[k] = 1.125 * double(k / 4) / double(s);
+    }
+    ts.deltatime = (.5 * cbrt(hex_volume_host(xl, yl, zl))) / sqrt(2.0 * einit);
+}
+
+void HostDomain::regions() {
+    std::vector<RegionRun> runs;
+    region_runs(numElem, numReg, balance, runs);
+    for (const RegionRun& r : runs) std::fill_n(regNumList.begin() + r.first, r.count, r.reg);
 }
 
 void HostDomain::symmetry() {
@@ -207,16 +264,8 @@ void HostDomain::build(int s_, int nr, int balance_, int cost_, double energy_sc
     symmetry();
     connectivity();
 
-    ts = lulesh_time_state{};
-    ts.dtfixed = -1.0e-6;
-    ts.stoptime = 1.0e-2;
-    ts.deltatimemultlb = 1.1;
-    ts.deltatimemultub = 1.2;
-    ts.dtcourant = 1.0e+20;
-    ts.dthydro = 1.0e+20;
-    ts.dtmax = 1.0e-2;
-    ts.time = 0.0;
-    ts.cycle = 0;
+    double einit = 0.0;
+    initial_time_state(s, energy_scale, ts, einit);
 
     for (int el = 0; el < numElem; ++el) {
         double xl[8], yl[8], zl[8];
@@ -231,12 +280,7 @@ void HostDomain::build(int s_, int nr, int balance_, int cost_, double energy_sc
         elemMass[el] = vol;
         for (int k = 0; k < 8; ++k) nodalMass[c[k]] += vol / 8.0;
     }
-    const double ebase = 3.948746e+7;
-    const double scale = s / 45.0;
-    double einit = ebase * scale * scale * scale;
-    if (energy_scale != 1.0) einit = einit * energy_scale;
     e[0] = einit;
-    ts.deltatime = (.5 * cbrt(volo[0])) / sqrt(2.0 * einit);
     fill_view();
 }
 
@@ -266,26 +310,7 @@ void HostDomain::fill_view() {
     w.nodeElemStart = nodeElemStart.data();
     w.nodeElemCornerList = nodeElemCornerList.data();
     w.regNumList = regNumList.data();
-    lulesh_params& P = w.params;
-    P.e_cut = 1.0e-7;
-    P.p_cut = 1.0e-7;
-    P.q_cut = 1.0e-7;
-    P.v_cut = 1.0e-10;
-    P.u_cut = 1.0e-7;
-    P.hgcoef = 3.0;
-    P.ss4o3 = 4.0 / 3.0;
-    P.qstop = 1.0e+12;
-    P.monoq_max_slope = 1.0;
-    P.monoq_limiter_mult = 2.0;
-    P.qlc_monoq = 0.5;
-    P.qqc_monoq = 2.0 / 3.0;
-    P.qqc = 2.0;
-    P.eosvmax = 1.0e+9;
-    P.eosvmin = 1.0e-9;
-    P.pmin = 0.0;
-    P.emin = -1.0e+15;
-    P.dvovmax = 0.1;
-    P.refdens = 1.0;
+    default_params(w.params);
     w.time = &ts;
 }
 

@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "lulesh_gb300.h"
 
 namespace lulesh {
@@ -176,6 +178,43 @@ int batch_occupancy(int phase, int block);
 int launch_batch_time_increment(const BatchCtl& c, cudaStream_t s);
 int launch_batch_time_finish(const BatchCtl& c, cudaStream_t s);
 
+// Final report on the device (verify.cu): out[0..3] = e(0), MaxAbsDiff,
+// TotalAbsDiff, MaxRelDiff of an nx^3 energy field; one block.
+int launch_verify(const double* e, int nx, double* out, cudaStream_t s);
+
+// --- problem set-up shared by the host Domain and the device build ---------------
+
+// EOS repeat count of a 0-based region (lulesh.cc:2156-2170).
+__host__ __device__ inline int region_rep(int reg, int numReg, int cost) {
+    if (reg < numReg / 2) return 1;
+    if (reg < (numReg - (numReg + 15) / 20)) return 1 + cost;
+    return 10 * (1 + cost);
+}
+
+// A run of consecutive elements of one region; reg is 1-based.
+struct RegionRun {
+    int32_t first, count, reg;
+};
+
+// The reference's region assignment (CreateRegionIndexSets,
+// lulesh-init.cc:341-445) as runs in element order: srand(0) and the
+// reference's sequence of rand() draws (domain.cpp).
+void region_runs(int numElem, int numReg, int balance, std::vector<RegionRun>& runs);
+// Physics constants of Domain::Domain (lulesh-init.cc:18-41).
+void default_params(lulesh_params& P);
+// Initial time state of an s^3 Sedov problem and its origin energy
+// (lulesh-init.cc:133-183); energy_scale multiplies the deposit.
+void initial_time_state(int s, double energy_scale, lulesh_time_state& ts, double& einit);
+
+// Device build of the initial state of problem s (device_init.cu): every
+// array of a carved mesh from the analytic cube, the region runs expanded
+// into elemRep and matOrder. `runs` are in element order, `order` lists
+// (first, count) element ranges in matOrder order with prefix offsets
+// `order_off` (norder + 1 entries); all three in device memory.
+int launch_build(const Mesh& m, int s, double einit, const RegionRun* runs, int nruns,
+                 const int2* order, const int32_t* order_off, int norder, int numReg, int cost,
+                 cudaStream_t st);
+
 // Handle-independent instance set-up shared by the single-problem handle and
 // the batch pool (capi.cu).
 size_t mesh_bytes(int precision, int numElem, int numNode);
@@ -184,6 +223,18 @@ int validate_view(const lulesh_domain_view* v);
 // the full state of v on stream s and waits for the copies; leaves
 // partials/result/dtime/matGrid to the caller.
 int mesh_init(Mesh& m, char* base, const lulesh_domain_view* v, int precision, cudaStream_t s);
+// Checks a problem description (sizes that fit the int32 indices).
+int check_problem(const lulesh_problem* p);
+// Builds problem p on the device into an already carved mesh with numElem
+// and numNode set (the build kernels, then a wait); fills *ts and, when
+// given, *classes as mesh_init_problem does.
+int mesh_fill_problem(Mesh& m, const lulesh_problem* p, int precision, cudaStream_t s, lulesh_time_state* ts,
+                      std::vector<int2>* classes);
+// The same for problem p built on the device (no host Domain): fills *ts
+// with the problem's initial time state and *classes with (repeat count,
+// elements) pairs, largest repeat count first; waits for the build.
+int mesh_init_problem(Mesh& m, char* base, const lulesh_problem* p, int precision, cudaStream_t s,
+                      lulesh_time_state* ts, std::vector<int2>* classes);
 // Copies the LULESH_F_* field groups of mask between m and v (either way)
 // on stream s and waits.
 int copy_fields(const Mesh& m, const lulesh_domain_view* v, uint32_t mask, bool to_device, cudaStream_t s);

@@ -1,21 +1,19 @@
 // Serving loop with continuous batching on top of the batch pool.
 //
-// Two host threads. The preparation thread waits for each request's arrival
-// time and builds its Domain on the host (the reference's set-up, which is
-// the slow part of admission for large s). The serving thread admits built
-// requests into the resident batch as slots and pool memory free up, replays
+// One host thread. Requests whose arrival time has passed queue up in
+// arrival order; the loop admits them into the resident batch as slots and
+// pool memory free up (each problem built directly in its pool block by the
+// device build, so admission costs milliseconds and no host Domain), replays
 // cycles of every resident problem from the batch's CUDA graph in chunks of
 // about sync_ms of device time (the chunk adapts to the measured cycle time),
-// and retires finished problems. Requests that arrive while others run join
-// the next chunk, so their work overlaps on the device with the problems
-// already resident.
+// and retires finished problems with their final report computed on the
+// device. Requests that arrive while others run join the next chunk, so
+// their work overlaps on the device with the problems already resident.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
-#include <condition_variable>
 #include <deque>
 #include <map>
-#include <mutex>
 #include <numeric>
 #include <thread>
 #include <vector>
@@ -23,11 +21,6 @@
 #include "lulesh_dev.h"
 
 namespace {
-
-struct Built {
-    int idx;
-    lulesh_domain* dom;
-};
 
 double quantile(std::vector<double> v, double q) {  // nearest rank
     if (v.empty()) return 0.0;
@@ -68,69 +61,42 @@ extern "C" int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_
     const auto t0 = clock::now();
     auto now_s = [&] { return std::chrono::duration<double>(clock::now() - t0).count(); };
 
-    std::mutex mu;
-    std::condition_variable cv;
-    std::deque<Built> ready;
-    bool stop = false;
-    int prep_error = LULESH_OK;
-    std::thread prep([&] {
-        for (int idx : order) {
-            for (;;) {
-                std::unique_lock<std::mutex> lk(mu);
-                if (stop) return;
-                const double wait = reqs[idx].arrival_s - now_s();
-                if (wait <= 0) break;
-                cv.wait_for(lk, std::chrono::duration<double>(std::min(wait, 0.05)));
-            }
-            const lulesh_problem& p = reqs[idx].problem;
-            lulesh_domain* dom = nullptr;
-            const int e = lulesh_domain_create(p.s, p.nr, p.balance, p.cost, p.energy_scale, &dom);
-            std::lock_guard<std::mutex> lk(mu);
-            if (e != LULESH_OK) {
-                prep_error = e;
-                cv.notify_all();
-                return;
-            }
-            ready.push_back({idx, dom});
-            cv.notify_all();
-        }
-    });
-
+    size_t next = 0;              // next request (arrival order) not yet queued
+    std::deque<int> pending;      // arrived, waiting for a slot and pool memory
     std::map<int, int> inflight;  // slot -> request
     std::vector<lulesh_slot_status> status(max_slots);
     int done = 0, chunk = 8, max_resident = 0;
     double device_ms = 0.0;
     while (st == LULESH_OK && done < n) {
-        {
-            std::unique_lock<std::mutex> lk(mu);
-            if (prep_error != LULESH_OK) {
-                st = prep_error;
-                break;
-            }
-            for (auto it = ready.begin(); it != ready.end();) {
-                const lulesh_problem& p = reqs[it->idx].problem;
-                int32_t slot = -1;
-                const int a = lulesh_batch_admit_view(b, lulesh_domain_get_view(it->dom), p.stoptime,
-                                                      p.max_cycles, &slot);
-                if (a == LULESH_ENOMEM) {  // not yet: a later, smaller request may fit
-                    ++it;
-                    continue;
-                }
-                if (a != LULESH_OK) {
-                    st = a;
-                    break;
-                }
-                results[it->idx].admitted_s = now_s();
-                inflight[slot] = it->idx;
-                lulesh_domain_destroy(it->dom);
-                it = ready.erase(it);
-            }
-            if (st != LULESH_OK) break;
-            max_resident = std::max(max_resident, int(inflight.size()));
-            if (inflight.empty()) {
-                cv.wait_for(lk, std::chrono::milliseconds(2));
+        const double t = now_s();
+        while (next < order.size() && reqs[order[next]].arrival_s <= t) pending.push_back(order[next++]);
+        // admit in arrival order; one that does not fit yet waits while later,
+        // smaller ones may go first
+        for (auto it = pending.begin(); it != pending.end();) {
+            int32_t slot = -1;
+            const int a = lulesh_batch_admit(b, &reqs[*it].problem, &slot);
+            if (a == LULESH_ENOMEM) {
+                ++it;
                 continue;
             }
+            if (a != LULESH_OK) {
+                st = a;
+                break;
+            }
+            results[*it].admitted_s = now_s();
+            inflight[slot] = *it;
+            it = pending.erase(it);
+        }
+        if (st != LULESH_OK) break;
+        max_resident = std::max(max_resident, int(inflight.size()));
+        if (inflight.empty()) {
+            // nothing resident (every request fits the empty pool, so none is
+            // pending): sleep until the next arrival, in short steps
+            if (next < order.size()) {
+                const double wait = reqs[order[next]].arrival_s - now_s();
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
+            }
+            continue;
         }
         int32_t active = 0;
         double ms = 0.0;
@@ -153,20 +119,19 @@ extern "C" int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_
             r.cycles = ss.cycle;
             r.err = ss.err;
             r.zone_cycles = int64_t(ss.numElem) * ss.cycle;
-            st = lulesh_batch_origin_energy(b, it->first, &r.e0);
+            // the final report on the device: no field leaves the GPU
+            lulesh_verify_result vr{};
+            st = lulesh_batch_verify(b, it->first, &vr);
+            r.e0 = vr.e0;
+            r.maxabs = vr.maxabs;
+            r.totabs = vr.totabs;
+            r.maxrel = vr.maxrel;
             if (st == LULESH_OK) st = lulesh_batch_retire(b, it->first);
             if (st != LULESH_OK) break;
             it = inflight.erase(it);
             ++done;
         }
     }
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        stop = true;
-        cv.notify_all();
-    }
-    prep.join();
-    for (Built& x : ready) lulesh_domain_destroy(x.dom);
     const int64_t launches = lulesh_batch_launch_count(b);
     lulesh_batch_destroy(b);
     if (st != LULESH_OK) return st;

@@ -51,6 +51,10 @@ def test_each_problem_equals_its_solo_run(lulesh, precision):
         alone, n = _alone(lulesh, precision, **sp)
         assert st[slot]["cycle"] == n and st[slot]["err"] == 0
         _assert_same(b.download(slot), alone)
+        # final report of the slot computed on the device
+        vr = b.verify(slot)
+        assert vr["cycle"] == n and vr["nx"] == sp["s"] and vr["e0"] == alone.e[0]
+        assert (vr["maxabs"], vr["totabs"], vr["maxrel"]) == alone.symmetry()
     assert b.launches > 0
 
 

@@ -102,6 +102,48 @@ def test_fp64_s90_1000_cycles_vs_reference(lulesh, golden_results):
         assert got <= SYM_FACTOR * want + 1e-300, (sym, ref)
 
 
+@pytest.mark.parametrize("precision", ["fp64_exact", "fp64", "mixed"])
+def test_device_final_report_equals_host(lulesh, golden_results, precision):
+    """lulesh_dev_verify (the final report computed on the device) equals
+    lulesh_symmetry on the downloaded energy field bit for bit; for the exact
+    variant at s=12 r=21 it also reproduces the reference's report."""
+    dom, dev, n = _run_device(lulesh, 12, 21, 1, 1, precision)
+    vr = dev.verify()
+    assert vr["cycle"] == n == dom.cycle and vr["nx"] == 12
+    assert vr["e0"] == dom.e[0]
+    assert (vr["maxabs"], vr["totabs"], vr["maxrel"]) == dom.symmetry()
+    if precision == "fp64_exact":
+        g = _golden(golden_results, 12, r=21)
+        assert n == g["cycles"]
+        assert abs(vr["e0"] - float(g["e0"])) <= 1e-13 * float(g["e0"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_s150_r21_to_stoptime_vs_oracle(lulesh, precision):
+    """The spec configuration run whole: s=150 r=21 (3,375,000
+    elements) to stoptime through the CUDA-graph time loop, against the CPU
+    oracle's run (tests/golden/s150_r21.json): same cycle count; e(0) within
+    1e-10 (double) or 1e-6 (mixed); double symmetry diffs at the reference's
+    level. About a minute of GPU time for both."""
+    import json
+    from pathlib import Path
+
+    g = json.loads((Path(__file__).resolve().parent / "golden" / "s150_r21.json").read_text())
+    dom, dev, n = _run_device(lulesh, 150, 21, 1, 1, precision, graph=True)
+    assert n == dom.cycle == g["cycles"]
+    vr = dev.verify()
+    assert vr["e0"] == dom.e[0] and (vr["maxabs"], vr["totabs"], vr["maxrel"]) == dom.symmetry()
+    e0 = float(g["e0"])
+    assert abs(dom.e[0] - e0) / e0 <= (E0_TOL_FP64 if precision == "fp64" else E0_TOL_MIXED)
+    if precision == "fp64":
+        sym = dom.symmetry()
+        ref = (float(g["maxabs"]), float(g["totabs"]), float(g["maxrel"]))
+        for got, want in zip(sym, ref):
+            assert got <= SYM_FACTOR * want + 1e-300, (sym, ref)
+    dev.close()
+    dom.close()
+
+
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-5)])
 def test_each_phase_after_one_cycle(lulesh, oracle_mod, precision, tol):
     """Kernel-by-kernel check on cycle 2 (cycle 1 has zero velocities): each

@@ -2,9 +2,10 @@
 
 Requests arrive on a seeded Poisson schedule while earlier ones are running;
 the loop admits them as slots and pool memory free up and retires each at its
-stoptime. Every request's result (cycle count and final origin energy) must
-be the same as the same problem run alone - bit for bit, since each problem
-keeps its own dt and exact dt minima inside the batch.
+stoptime. Every request's result (cycle count, final origin energy and the
+plane-0 symmetry diffs computed on the device) must be the same as the same
+problem run alone - bit for bit, since each problem keeps its own dt and
+exact dt minima inside the batch.
 """
 from __future__ import annotations
 
@@ -29,7 +30,7 @@ def _solo(lulesh, precision, req):
     dev = lulesh.Device(dom, precision)
     n = dev.run()
     dev.download()
-    return n, float(dom.e[0])
+    return n, float(dom.e[0]), dom.symmetry()
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
@@ -44,9 +45,11 @@ def test_each_request_equals_its_solo_run(lulesh, precision):
         assert res["admitted_s"] >= req["arrival_s"] - 1e-9
         assert res["finished_s"] >= res["admitted_s"]
         assert res["time_to_solution_s"] == pytest.approx(res["finished_s"] - req["arrival_s"])
-        n, e0 = _solo(lulesh, precision, req)
+        n, e0, sym = _solo(lulesh, precision, req)
         assert res["cycles"] == n
         assert res["e0"] == e0
+        # the symmetry check is computed on the device at retire
+        assert (res["maxabs"], res["totabs"], res["maxrel"]) == sym
         assert res["zone_cycles"] == req["s"] ** 3 * n
     assert 0 < stats["p50_s"] <= stats["p99_s"]
     assert stats["zone_cycles"] == sum(r["zone_cycles"] for r in results)
