@@ -505,7 +505,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--size", type=int, default=150)
     ap.add_argument("--regions", type=int, default=21)
-    ap.add_argument("--cpu-cycles", type=int, default=20)
+    ap.add_argument("--cpu-cycles", type=int, default=120)
     ap.add_argument("--skip-mixed", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")

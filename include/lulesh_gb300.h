@@ -189,7 +189,11 @@ int lulesh_dev_step(lulesh_dev* dev, double deltatime, double* dtcourant, double
 /* The literal drop-in for LagrangeLeapFrogWithTasks(Domain&): uploads the
  * state a step reads from the host Domain view, runs one cycle with
  * view->time->deltatime, downloads every field the step writes and stores
- * dtcourant/dthydro into view->time. */
+ * dtcourant/dthydro into view->time. The copies overlap the cycle: the
+ * upload runs on two streams, node fields stream back while the element
+ * phases run and the kinematic fields while the material phase runs. On
+ * LULESH_EVOLUME (where the reference exits) the host fields hold the
+ * partly advanced state and view->time's dt constraints are unchanged. */
 int lulesh_leapfrog(lulesh_dev* dev, lulesh_domain_view* host);
 
 /* The time loop of hpx_main (lulesh.cc:2374-2386) on device-resident state:

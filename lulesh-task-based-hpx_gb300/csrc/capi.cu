@@ -69,6 +69,9 @@ struct lulesh_dev {
     int32_t nx = 0;                  // edge of the cube (Domain::sizeX)
     double* d_verify = nullptr;      // [4] lulesh_dev_verify output (arena)
     double* h_verify = nullptr;      // [4] pinned
+    // lulesh_leapfrog's second copy stream and its hand-off events (created on first use)
+    cudaStream_t cstream = nullptr;
+    cudaEvent_t ev_up = nullptr, ev_e = nullptr, ev_nodes = nullptr, ev_kin = nullptr;
     Launchers L{};
     // device-side timing (lulesh_dev_profile_begin/end)
     bool profiling = false;
@@ -421,6 +424,10 @@ void lulesh_dev_destroy(lulesh_dev* d) {
     if (d->h_result) cudaFreeHost(d->h_result);
     if (d->h_time) cudaFreeHost(d->h_time);
     if (d->h_verify) cudaFreeHost(d->h_verify);
+    if (d->cstream) cudaStreamSynchronize(d->cstream);
+    for (cudaEvent_t e : {d->ev_up, d->ev_e, d->ev_nodes, d->ev_kin})
+        if (e) cudaEventDestroy(e);
+    if (d->cstream) cudaStreamDestroy(d->cstream);
     if (d->stream) cudaStreamDestroy(d->stream);
     delete d;
 }
@@ -477,12 +484,70 @@ int lulesh_dev_step(lulesh_dev* d, double dt, double* dtcourant, double* dthydro
 }
 
 int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
-    if (!d || !v || !v->time) return LULESH_EINVAL;
-    int st = lulesh_dev_upload(d, v, LULESH_F_STEP_IN);
-    if (st != LULESH_OK) return st;
-    st = lulesh_dev_step(d, v->time->deltatime, &v->time->dtcourant, &v->time->dthydro);
-    if (st != LULESH_OK) return st;
-    return lulesh_dev_download(d, v, LULESH_F_STEP_OUT);
+    if (!d || !v || !v->time || v->numElem != d->m.numElem || v->numNode != d->m.numNode)
+        return LULESH_EINVAL;
+    if (!(v->time->deltatime > 0.0)) return LULESH_EINVAL;
+    const auto in = groups(d->m, v, LULESH_F_STEP_IN);
+    const auto out_nodes = groups(d->m, v, LULESH_F_POS | LULESH_F_VEL | LULESH_F_ACC | LULESH_F_FORCE);
+    const auto out_kin = groups(d->m, v, LULESH_F_V | LULESH_F_KIN);
+    const auto out_mat = groups(d->m, v, LULESH_F_EPQ | LULESH_F_QLQQ | LULESH_F_SS);
+    for (const auto* g : {&in, &out_nodes, &out_kin, &out_mat})
+        for (const Copy& c : *g)
+            if (!c.host) return LULESH_EINVAL;
+    if (!d->cstream) {
+        CK(cudaStreamCreateWithFlags(&d->cstream, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&d->ev_up, &d->ev_e, &d->ev_nodes, &d->ev_kin})
+            CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    const Mesh& m = d->m;
+    const double dt = v->time->deltatime;
+    // Upload the step inputs on both streams (two copy engines), then run the
+    // cycle; the energy, read only by the material phase, uploads while the
+    // earlier phases run. The fields each phase leaves final go back on the
+    // copy stream while the later phases run: node fields after the node
+    // kernel, volumes and kinematics after the kinematics kernel. Only the
+    // material phase's outputs are copied after the cycle.
+    const Copy* e_in = nullptr;
+    int k = 0;
+    for (const Copy& c : in) {
+        if (c.dev == m.e) {
+            e_in = &c;
+            continue;
+        }
+        CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, (k++ & 1) ? d->cstream : d->stream));
+    }
+    CK(cudaEventRecord(d->ev_up, d->cstream));
+    CK(cudaStreamWaitEvent(d->stream, d->ev_up, 0));
+    if (e_in) CK(cudaMemcpyAsync(e_in->dev, e_in->host, e_in->bytes, cudaMemcpyHostToDevice, d->cstream));
+    CK(cudaEventRecord(d->ev_e, d->cstream));
+    if (d->precision == LULESH_MIXED) d->launches += lulesh::mixed::launch_mirror(m, d->stream);
+    CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
+    d->launches += d->L.forces(m, d->stream);
+    d->launches += d->L.nodes(m, dt, d->stream);
+    CK(cudaEventRecord(d->ev_nodes, d->stream));
+    d->launches += d->L.kinematics(m, dt, d->stream);
+    CK(cudaEventRecord(d->ev_kin, d->stream));
+    CK(cudaStreamWaitEvent(d->stream, d->ev_e, 0));
+    d->launches += d->L.material(m, d->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamWaitEvent(d->cstream, d->ev_nodes, 0));
+    for (const Copy& c : out_nodes)
+        CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->cstream));
+    CK(cudaStreamWaitEvent(d->cstream, d->ev_kin, 0));
+    for (const Copy& c : out_kin)
+        CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->cstream));
+    CK(cudaMemcpyAsync(d->h_result, m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
+    for (const Copy& c : out_mat)
+        CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->stream));
+    CK(cudaStreamSynchronize(d->stream));
+    CK(cudaStreamSynchronize(d->cstream));
+    if (d->h_result->err != 0) {
+        d->err_elem = d->h_result->err_elem;
+        return d->h_result->err;
+    }
+    v->time->dtcourant = d->h_result->dtcourant;
+    v->time->dthydro = d->h_result->dthydro;
+    return LULESH_OK;
 }
 
 int lulesh_dev_run(lulesh_dev* d, lulesh_time_state* ts, int32_t max_cycles, int32_t* cycles_run) {

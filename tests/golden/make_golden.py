@@ -10,10 +10,17 @@ the sequential HPX stand-in into oracle/_ref/lulesh-ref (-O3
                  computes them (lulesh-util.cc:60-115)
   dump_*.npz     every node and element field after a fixed number of cycles
 
+  s150_r21.json  the s=150 r=21 run to stoptime (5,382 cycles, about 1.7e10
+                 zone-cycles): hours for the single-threaded reference binary,
+                 so it comes from the oracle port with OpenMP threads, which
+                 equals the reference binary byte for byte on every golden run
+                 and dump (tests/test_oracle.py) at any thread count
+
 Needs the reference sources, so it runs in the build container only; the
 fixtures it writes are committed and used everywhere else.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py           # results.json and the dumps
+    python tests/golden/make_golden.py --s150    # s150_r21.json (about 30 min on 8 cores)
 """
 from __future__ import annotations
 
@@ -57,7 +64,25 @@ def run_ref(s, r, b, c, its=None, dump=None) -> dict:
             "time": kv["time"], "dt": kv["dt"]}
 
 
+def run_s150(threads: int) -> dict:
+    """The s=150 r=21 run to stoptime through the oracle port's command line
+    (the reference's flags and report fields)."""
+    oracle.build(ref=False)
+    args = [str(oracle.HERE / "lulesh-oracle"), "--s", "150", "--r", "21", "--threads", str(threads)]
+    out = subprocess.run(args, capture_output=True, text=True, check=True).stdout
+    kv = dict(t.split("=", 1) for t in _RES.search(out).group(1).split())
+    return {"s": 150, "r": 21, "b": 1, "c": 1, "cycles": int(kv["cycles"]), "e0": kv["e0"],
+            "maxabs": kv["maxabs"], "totabs": kv["totabs"], "maxrel": kv["maxrel"],
+            "time": kv["time"], "dt": kv["dt"], "source": "oracle port (lulesh-oracle), "
+            f"{threads} OpenMP threads, libm cube root", "command": " ".join(args[1:])}
+
+
 def main() -> None:
+    if "--s150" in sys.argv:
+        res = run_s150(os.cpu_count() or 1)
+        print(res, flush=True)
+        (HERE / "s150_r21.json").write_text(json.dumps(res, indent=1) + "\n")
+        return
     if not oracle.REF_SOURCES.is_dir():
         sys.exit("the reference sources are needed to generate the fixtures")
     oracle.build(ref=True)

@@ -194,16 +194,20 @@ def test_run_to_run_determinism(lulesh, precision):
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
 
 
-def test_leapfrog_on_host_buffers_equals_resident_run(lulesh):
+@pytest.mark.parametrize("precision", ["fp64", "fp64_exact", "mixed"])
+def test_leapfrog_on_host_buffers_equals_resident_run(lulesh, precision):
     """lulesh_leapfrog (upload, step, download each cycle, the literal
-    drop-in for LagrangeLeapFrog(Domain&)) gives the device-resident bits."""
+    drop-in for LagrangeLeapFrog(Domain&), its copies overlapping the
+    cycle) gives the device-resident bits, dt constraints included."""
     a = lulesh.HostDomain(10)
-    dev_a = lulesh.Device(a, "fp64")
+    dev_a = lulesh.Device(a, precision)
     for _ in range(25):
         a.time_increment()
         dev_a.leapfrog()
-    b, _, n = _run_device(lulesh, 10, 11, 1, 1, "fp64", its=25)
+    b, _, n = _run_device(lulesh, 10, 11, 1, 1, precision, its=25)
     assert a.cycle == b.cycle == n == 25
+    for f in ("time", "deltatime", "dtcourant", "dthydro"):
+        assert getattr(a.time_state, f) == getattr(b.time_state, f), f
     for f in NODE + ELEM:
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
 
