@@ -459,7 +459,7 @@ int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot_o
         b->pool.release(off, bytes);
         return st;
     }
-    b->launches += b->precision == LULESH_MIXED ? 5 : 4;
+    b->launches += b->precision == LULESH_MIXED ? 6 : 5;  // the build kernels, the order (and the mirror)
     return finish_admit(b, slot, off, bytes, m, ts, p->stoptime, p->max_cycles, classes, p->s, slot_out);
 }
 

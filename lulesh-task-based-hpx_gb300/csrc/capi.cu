@@ -22,19 +22,24 @@ struct Launchers {
     int (*nodes)(const Mesh&, double, cudaStream_t);
     int (*kinematics)(const Mesh&, double, cudaStream_t);
     int (*material)(const Mesh&, cudaStream_t);
+    int (*forces_range)(const Mesh&, int, int, cudaStream_t);
+    int (*material_range)(const Mesh&, int, int, bool, cudaStream_t);
 };
 
 Launchers launchers_for(int precision) {
     switch (precision) {
         case LULESH_FP64:
             return {lulesh::fp64::launch_forces, lulesh::fp64::launch_nodes,
-                    lulesh::fp64::launch_kinematics, lulesh::fp64::launch_material};
+                    lulesh::fp64::launch_kinematics, lulesh::fp64::launch_material,
+                    lulesh::fp64::launch_forces_range, lulesh::fp64::launch_material_range};
         case LULESH_FP64_EXACT:
             return {lulesh::fp64x::launch_forces, lulesh::fp64x::launch_nodes,
-                    lulesh::fp64x::launch_kinematics, lulesh::fp64x::launch_material};
+                    lulesh::fp64x::launch_kinematics, lulesh::fp64x::launch_material,
+                    lulesh::fp64x::launch_forces_range, lulesh::fp64x::launch_material_range};
         default:
             return {lulesh::mixed::launch_forces, lulesh::mixed::launch_nodes,
-                    lulesh::mixed::launch_kinematics, lulesh::mixed::launch_material};
+                    lulesh::mixed::launch_kinematics, lulesh::mixed::launch_material,
+                    lulesh::mixed::launch_forces_range, lulesh::mixed::launch_material_range};
     }
 }
 
@@ -72,6 +77,9 @@ struct lulesh_dev {
     // lulesh_leapfrog's second copy stream and its hand-off events (created on first use)
     cudaStream_t cstream = nullptr;
     cudaEvent_t ev_up = nullptr, ev_e = nullptr, ev_nodes = nullptr, ev_kin = nullptr;
+    std::vector<cudaEvent_t> ev_slab, ev_mat;  // one per slab: upload done, material done
+    cudaStream_t mstream = nullptr;            // downloads of the material phase's outputs
+    int32_t* matOrderSlab = nullptr;           // [N_e] slab-major material order (arena)
     Launchers L{};
     // device-side timing (lulesh_dev_profile_begin/end)
     bool profiling = false;
@@ -80,6 +88,21 @@ struct lulesh_dev {
     double kernel_ms[4] = {0, 0, 0, 0};
     int64_t prof_cycles = 0, prof_launch0 = 0;
 };
+
+// Upload slabs of lulesh_leapfrog (element planes per slab = s / slabs).
+constexpr int kLeapfrogSlabs = 8;
+
+// Slabs of a handle's problem: whole element planes of the cube of edge s
+// (one slab when the mesh is not an s^3 cube).
+int slab_count(int s, int64_t numElem) {
+    const bool cube = s >= 1 && int64_t(s) * s * s == numElem;
+    return cube ? std::min(s, kLeapfrogSlabs) : 1;
+}
+// Element planes [p0, p1) of slab sl.
+void slab_planes(int s, int slabs, int sl, int& p0, int& p1) {
+    p0 = int(int64_t(s) * sl / slabs);
+    p1 = int(int64_t(s) * (sl + 1) / slabs);
+}
 
 #define CK(call)                                          \
     do {                                                  \
@@ -173,6 +196,7 @@ void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     m.result = a.take<StepResult>(1);
     d->d_time = a.take<DevTime>(1);
     d->d_verify = a.take<double>(4);
+    d->matOrderSlab = a.take<int32_t>(ne);
 }
 
 struct Copy {
@@ -222,7 +246,8 @@ std::vector<Copy> groups(const Mesh& m, const lulesh_domain_view* v, uint32_t ma
 // mutable state of v into the carved mesh m, refreshes the mixed path's
 // float-pair mirrors, and waits for the copies (some read host vectors that
 // live only in this call).
-int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaStream_t s) {
+int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaStream_t s, int slabs,
+                int32_t* slab_order) {
     const int ne = v->numElem, nn = v->numNode;
     // per-node symmetry bits, per-element EOS repeat count and the
     // repeat-count grouping of the material phase
@@ -236,6 +261,22 @@ int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaS
     for (int i = 0; i < ne; ++i) rep[i] = lulesh::region_rep(v->regNumList[i] - 1, v->numReg, v->cost);
     for (int i = 0; i < ne; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rep[a] > rep[b]; });
+    std::vector<int32_t> sorder;
+    if (slab_order && slabs > 1) {
+        // the same order split by slab of whole element planes (a stable
+        // partition: repeat-count order within each slab)
+        const int sx = v->sizeX, s2 = sx * sx;
+        std::vector<int> slab_of(sx);
+        for (int sl = 0; sl < slabs; ++sl) {
+            int p0, p1;
+            slab_planes(sx, slabs, sl, p0, p1);
+            for (int pl = p0; pl < p1; ++pl) slab_of[pl] = sl;
+        }
+        sorder = order;
+        std::stable_sort(sorder.begin(), sorder.end(),
+                         [&](int a, int b) { return slab_of[a / s2] < slab_of[b / s2]; });
+        CK(cudaMemcpyAsync(slab_order, sorder.data(), sizeof(int32_t) * size_t(ne), cudaMemcpyHostToDevice, s));
+    }
 
     const size_t eb = sizeof(int32_t) * size_t(ne);
     const Copy consts[] = {
@@ -381,7 +422,7 @@ int lulesh_dev_create(const lulesh_domain_view* v, int32_t precision, lulesh_dev
     if (st != LULESH_OK) return st;
     d->m.prm = v->params;
     d->nx = v->sizeX;
-    st = upload_mesh(d->m, v, precision, d->stream);
+    st = upload_mesh(d->m, v, precision, d->stream, slab_count(v->sizeX, v->numElem), d->matOrderSlab);
     if (st != LULESH_OK) {
         lulesh_dev_destroy(d);
         return st;
@@ -402,12 +443,14 @@ int lulesh_dev_create_problem(const lulesh_problem* p, int32_t precision, lulesh
     st = new_handle(precision, ne, nn, &d);
     if (st != LULESH_OK) return st;
     d->nx = p->s;
-    st = lulesh::mesh_fill_problem(d->m, p, precision, d->stream, ts, nullptr);
+    st = lulesh::mesh_fill_problem(d->m, p, precision, d->stream, ts, nullptr, slab_count(p->s, ne),
+                                   d->matOrderSlab);
     if (st != LULESH_OK) {
         lulesh_dev_destroy(d);
         return st;
     }
-    d->launches += precision == LULESH_MIXED ? 5 : 4;  // the build kernels (and the mirror)
+    // the build kernels, the material orders (and the mirror)
+    d->launches += 5 + (slab_count(p->s, ne) > 1 ? 1 : 0) + (precision == LULESH_MIXED ? 1 : 0);
     *out = d;
     return LULESH_OK;
 }
@@ -427,6 +470,12 @@ void lulesh_dev_destroy(lulesh_dev* d) {
     if (d->cstream) cudaStreamSynchronize(d->cstream);
     for (cudaEvent_t e : {d->ev_up, d->ev_e, d->ev_nodes, d->ev_kin})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : d->ev_slab) cudaEventDestroy(e);
+    for (cudaEvent_t e : d->ev_mat) cudaEventDestroy(e);
+    if (d->mstream) {
+        cudaStreamSynchronize(d->mstream);
+        cudaStreamDestroy(d->mstream);
+    }
     if (d->cstream) cudaStreamDestroy(d->cstream);
     if (d->stream) cudaStreamDestroy(d->stream);
     delete d;
@@ -496,51 +545,97 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
             if (!c.host) return LULESH_EINVAL;
     if (!d->cstream) {
         CK(cudaStreamCreateWithFlags(&d->cstream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&d->mstream, cudaStreamNonBlocking));
         for (cudaEvent_t* e : {&d->ev_up, &d->ev_e, &d->ev_nodes, &d->ev_kin})
             CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     const Mesh& m = d->m;
     const double dt = v->time->deltatime;
-    // Upload the step inputs on both streams (two copy engines), then run the
-    // cycle; the energy, read only by the material phase, uploads while the
-    // earlier phases run. The fields each phase leaves final go back on the
-    // copy stream while the later phases run: node fields after the node
-    // kernel, volumes and kinematics after the kinematics kernel. Only the
-    // material phase's outputs are copied after the cycle.
-    const Copy* e_in = nullptr;
-    int k = 0;
-    for (const Copy& c : in) {
-        if (c.dev == m.e) {
-            e_in = &c;
-            continue;
+    // The cycle runs in slabs of whole element planes (the handle's matOrder
+    // is slab-major). The upload runs slab by slab on the copy stream, and
+    // the force kernel of a slab starts once its elements' inputs and its
+    // nodes (its planes and the next node plane) are on the device, so most
+    // of the upload overlaps the force phase; the energy, read only by the
+    // material phase, uploads last. The fields each phase leaves final go
+    // back while the later phases run: node fields after the node kernel and
+    // kinematic fields after the kinematics kernel (copy stream), each slab's
+    // material outputs after its material launch (third stream).
+    const int s = d->nx;
+    const int slabs = slab_count(s, m.numElem);
+    const bool cube = slabs > 1 || (s >= 1 && int64_t(s) * s * s == int64_t(m.numElem));
+    const int64_t plane_n = cube ? int64_t(s + 1) * (s + 1) : m.numNode;
+    const int64_t plane_e = cube ? int64_t(s) * s : m.numElem;
+    if (d->ev_slab.size() < size_t(slabs)) {
+        for (auto* evs : {&d->ev_slab, &d->ev_mat}) {
+            for (cudaEvent_t e : *evs) cudaEventDestroy(e);
+            evs->assign(slabs, nullptr);
+            for (cudaEvent_t& e : *evs) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
-        CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, (k++ & 1) ? d->cstream : d->stream));
     }
-    CK(cudaEventRecord(d->ev_up, d->cstream));
-    CK(cudaStreamWaitEvent(d->stream, d->ev_up, 0));
+    std::vector<int64_t> e_lo(slabs), e_hi(slabs), n_hi(slabs);
+    for (int sl = 0; sl < slabs; ++sl) {
+        int p0 = 0, p1 = 1;
+        if (cube) slab_planes(s, slabs, sl, p0, p1);
+        e_lo[sl] = cube ? p0 * plane_e : 0;
+        e_hi[sl] = cube ? p1 * plane_e : m.numElem;
+        n_hi[sl] = cube ? (p1 + 1) * plane_n : m.numNode;
+    }
+    CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
+    // the copy stream starts after the previous cycle's work on the compute stream
+    CK(cudaEventRecord(d->ev_up, d->stream));
+    CK(cudaStreamWaitEvent(d->cstream, d->ev_up, 0));
+    const Copy* e_in = nullptr;
+    int64_t node_done = 0;
+    for (int sl = 0; sl < slabs; ++sl) {
+        const int64_t e0 = e_lo[sl], e1 = e_hi[sl], n1 = n_hi[sl];
+        for (const Copy& c : in) {
+            if (c.dev == m.e) {
+                e_in = &c;
+                continue;
+            }
+            const bool node = c.bytes == sizeof(double) * size_t(m.numNode);
+            const int64_t a = node ? node_done : e0, b = node ? n1 : e1;
+            if (b > a)
+                CK(cudaMemcpyAsync(static_cast<double*>(c.dev) + a, static_cast<const double*>(c.host) + a,
+                                   sizeof(double) * size_t(b - a), cudaMemcpyHostToDevice, d->cstream));
+        }
+        CK(cudaEventRecord(d->ev_slab[sl], d->cstream));
+        CK(cudaStreamWaitEvent(d->stream, d->ev_slab[sl], 0));
+        if (d->precision == LULESH_MIXED)
+            d->launches += lulesh::mixed::launch_mirror_range(m, int(node_done), int(n1), d->stream);
+        d->launches += d->L.forces_range(m, int(e0), int(e1), d->stream);
+        node_done = n1;
+    }
     if (e_in) CK(cudaMemcpyAsync(e_in->dev, e_in->host, e_in->bytes, cudaMemcpyHostToDevice, d->cstream));
     CK(cudaEventRecord(d->ev_e, d->cstream));
-    if (d->precision == LULESH_MIXED) d->launches += lulesh::mixed::launch_mirror(m, d->stream);
-    CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
-    d->launches += d->L.forces(m, d->stream);
     d->launches += d->L.nodes(m, dt, d->stream);
     CK(cudaEventRecord(d->ev_nodes, d->stream));
     d->launches += d->L.kinematics(m, dt, d->stream);
     CK(cudaEventRecord(d->ev_kin, d->stream));
-    CK(cudaStreamWaitEvent(d->stream, d->ev_e, 0));
-    d->launches += d->L.material(m, d->stream);
-    CK(cudaGetLastError());
     CK(cudaStreamWaitEvent(d->cstream, d->ev_nodes, 0));
     for (const Copy& c : out_nodes)
         CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->cstream));
     CK(cudaStreamWaitEvent(d->cstream, d->ev_kin, 0));
     for (const Copy& c : out_kin)
         CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->cstream));
+    CK(cudaStreamWaitEvent(d->stream, d->ev_e, 0));
+    Mesh ms = m;  // the slab-major material order: positions [e_lo, e_hi) are the slab's elements
+    if (slabs > 1) ms.matOrder = d->matOrderSlab;
+    for (int sl = 0; sl < slabs; ++sl) {
+        d->launches += d->L.material_range(ms, int(e_lo[sl]), int(e_hi[sl]), sl > 0, d->stream);
+        CK(cudaEventRecord(d->ev_mat[sl], d->stream));
+        CK(cudaStreamWaitEvent(d->mstream, d->ev_mat[sl], 0));
+        const size_t off = size_t(e_lo[sl]), cnt = size_t(e_hi[sl] - e_lo[sl]);
+        for (const Copy& c : out_mat)
+            CK(cudaMemcpyAsync(const_cast<double*>(static_cast<const double*>(c.host)) + off,
+                               static_cast<double*>(c.dev) + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
+                               d->mstream));
+    }
+    CK(cudaGetLastError());
     CK(cudaMemcpyAsync(d->h_result, m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
-    for (const Copy& c : out_mat)
-        CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->stream));
     CK(cudaStreamSynchronize(d->stream));
     CK(cudaStreamSynchronize(d->cstream));
+    CK(cudaStreamSynchronize(d->mstream));
     if (d->h_result->err != 0) {
         d->err_elem = d->h_result->err_elem;
         return d->h_result->err;
@@ -738,7 +833,7 @@ int mesh_init(Mesh& m, char* base, const lulesh_domain_view* v, int precision, c
     m.numElem = v->numElem;
     m.numNode = v->numNode;
     m.prm = v->params;
-    return upload_mesh(m, v, precision, s);
+    return upload_mesh(m, v, precision, s, 1, nullptr);
 }
 
 int check_problem(const lulesh_problem* p) {
@@ -749,8 +844,31 @@ int check_problem(const lulesh_problem* p) {
     return LULESH_OK;
 }
 
+namespace {
+// Material order as (first, count) element ranges with prefix offsets:
+// the runs ordered by key(run) ascending, then repeat count descending
+// (a stable sort, so element order within equal keys).
+template <class Key>
+void order_ranges(const std::vector<RegionRun>& runs, const std::vector<int>& rep, Key key,
+                  std::vector<int2>& order, std::vector<int32_t>& off, std::vector<int>* idx_out = nullptr) {
+    const int n = int(runs.size());
+    std::vector<int> idx(n);
+    for (int r = 0; r < n; ++r) idx[r] = r;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+        return key(a) != key(b) ? key(a) < key(b) : rep[a] > rep[b];
+    });
+    order.resize(n);
+    off.assign(n + 1, 0);
+    for (int k = 0; k < n; ++k) {
+        order[k] = make_int2(runs[idx[k]].first, runs[idx[k]].count);
+        off[k + 1] = off[k] + runs[idx[k]].count;
+    }
+    if (idx_out) idx_out->swap(idx);
+}
+}  // namespace
+
 int mesh_fill_problem(Mesh& m, const lulesh_problem* p, int precision, cudaStream_t s, lulesh_time_state* ts,
-                      std::vector<int2>* classes) {
+                      std::vector<int2>* classes, int slabs, int32_t* slab_order) {
     const int ne = m.numElem;
     default_params(m.prm);
     double einit = 0.0;
@@ -761,43 +879,78 @@ int mesh_fill_problem(Mesh& m, const lulesh_problem* p, int precision, cudaStrea
     // phase's matOrder as (first, count) ranges
     std::vector<RegionRun> runs;
     region_runs(ne, p->nr, p->balance, runs);
-    const int nruns = int(runs.size());
-    std::vector<int> rep(nruns), idx(nruns);
-    for (int r = 0; r < nruns; ++r) {
-        rep[r] = region_rep(runs[r].reg - 1, p->nr, p->cost);
-        idx[r] = r;
-    }
-    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return rep[a] > rep[b]; });
-    std::vector<int2> order(nruns);
-    std::vector<int32_t> off(nruns + 1, 0);
-    for (int k = 0; k < nruns; ++k) {
-        order[k] = make_int2(runs[idx[k]].first, runs[idx[k]].count);
-        off[k + 1] = off[k] + runs[idx[k]].count;
-    }
+    std::vector<int> rep(runs.size());
+    for (size_t r = 0; r < runs.size(); ++r) rep[r] = region_rep(runs[r].reg - 1, p->nr, p->cost);
+    std::vector<int2> order;
+    std::vector<int32_t> off;
+    std::vector<int> idx;
+    order_ranges(runs, rep, [](int) { return 0; }, order, off, &idx);
     if (classes) {
         classes->clear();
-        for (int k = 0; k < nruns; ++k) {
+        for (size_t k = 0; k < idx.size(); ++k) {
             const int r = rep[idx[k]];
             if (classes->empty() || classes->back().x != r) classes->push_back(make_int2(r, 0));
             classes->back().y += runs[idx[k]].count;
         }
     }
-    // the three tables in one stream-ordered temporary allocation
-    const size_t b_runs = (sizeof(RegionRun) * nruns + 255) & ~size_t(255);
-    const size_t b_order = (sizeof(int2) * nruns + 255) & ~size_t(255);
-    const size_t b_off = sizeof(int32_t) * (nruns + 1);
+    // the slab-major order: runs cut at the slab boundaries (whole element
+    // planes), ordered by slab, then repeat count
+    std::vector<int2> sorder;
+    std::vector<int32_t> soff;
+    const bool with_slabs = slab_order && slabs > 1;
+    if (with_slabs) {
+        std::vector<int64_t> bound;
+        for (int sl = 1; sl < slabs; ++sl) {
+            int p0, p1;
+            slab_planes(p->s, slabs, sl, p0, p1);
+            bound.push_back(int64_t(p0) * p->s * p->s);
+        }
+        std::vector<RegionRun> cut;
+        std::vector<int> cut_rep, slab_of;
+        for (size_t r = 0; r < runs.size(); ++r) {
+            int64_t a = runs[r].first;
+            const int64_t end = a + runs[r].count;
+            int sl = int(std::upper_bound(bound.begin(), bound.end(), a) - bound.begin());
+            while (a < end) {
+                const int64_t b = sl < int(bound.size()) ? std::min(end, bound[sl]) : end;
+                cut.push_back({int32_t(a), int32_t(b - a), runs[r].reg});
+                cut_rep.push_back(rep[r]);
+                slab_of.push_back(sl);
+                a = b;
+                ++sl;
+            }
+        }
+        order_ranges(cut, cut_rep, [&](int k) { return slab_of[k]; }, sorder, soff);
+    }
+    // the tables in one stream-ordered temporary allocation
+    const int nruns = int(runs.size()), ncut = int(sorder.size());
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t b_runs = al(sizeof(RegionRun) * nruns), b_order = al(sizeof(int2) * nruns),
+                 b_off = al(sizeof(int32_t) * (nruns + 1)), b_sorder = al(sizeof(int2) * ncut),
+                 b_soff = al(sizeof(int32_t) * (ncut + 1));
     char* tab = nullptr;
-    CK(cudaMallocAsync(reinterpret_cast<void**>(&tab), b_runs + b_order + b_off, s));
+    CK(cudaMallocAsync(reinterpret_cast<void**>(&tab), b_runs + b_order + b_off + b_sorder + b_soff, s));
     RegionRun* d_runs = reinterpret_cast<RegionRun*>(tab);
     int2* d_order = reinterpret_cast<int2*>(tab + b_runs);
     int32_t* d_off = reinterpret_cast<int32_t*>(tab + b_runs + b_order);
+    int2* d_sorder = reinterpret_cast<int2*>(tab + b_runs + b_order + b_off);
+    int32_t* d_soff = reinterpret_cast<int32_t*>(tab + b_runs + b_order + b_off + b_sorder);
     int st = LULESH_OK;
-    if (cudaMemcpyAsync(d_runs, runs.data(), sizeof(RegionRun) * nruns, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(d_order, order.data(), sizeof(int2) * nruns, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(d_off, off.data(), b_off, cudaMemcpyHostToDevice, s) != cudaSuccess)
-        st = LULESH_ECUDA;
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (st == LULESH_OK && bytes && cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            st = LULESH_ECUDA;
+    };
+    up(d_runs, runs.data(), sizeof(RegionRun) * nruns);
+    up(d_order, order.data(), sizeof(int2) * nruns);
+    up(d_off, off.data(), sizeof(int32_t) * (nruns + 1));
+    if (with_slabs) {
+        up(d_sorder, sorder.data(), sizeof(int2) * ncut);
+        up(d_soff, soff.data(), sizeof(int32_t) * (ncut + 1));
+    }
     if (st == LULESH_OK) {
-        launch_build(m, p->s, einit, d_runs, nruns, d_order, d_off, nruns, p->nr, p->cost, s);
+        launch_build(m, p->s, einit, d_runs, nruns, p->nr, p->cost, s);
+        launch_build_order(const_cast<int32_t*>(m.matOrder), ne, d_order, d_off, nruns, s);
+        if (with_slabs) launch_build_order(slab_order, ne, d_sorder, d_soff, ncut, s);
         if (precision == LULESH_MIXED) mixed::launch_mirror(m, s);
         if (cudaGetLastError() != cudaSuccess) st = LULESH_ECUDA;
     }
@@ -814,7 +967,7 @@ int mesh_init_problem(Mesh& m, char* base, const lulesh_problem* p, int precisio
     carve_mesh(m, a, precision, ne, nn);
     m.numElem = ne;
     m.numNode = nn;
-    return mesh_fill_problem(m, p, precision, s, ts, classes);
+    return mesh_fill_problem(m, p, precision, s, ts, classes, 1, nullptr);
 }
 
 int copy_fields(const Mesh& m, const lulesh_domain_view* v, uint32_t mask, bool to_device, cudaStream_t s) {

@@ -138,12 +138,9 @@ __global__ void __launch_bounds__(kBuildBlock) k_build_mass(Mesh m, int s) {
     const_cast<double*>(m.invMass)[n] = 1.0 / mass;
 }
 
-// elemRep from the region runs (element order) and matOrder from the
-// (first, count) ranges in repeat-count order; both by binary search.
-__global__ void __launch_bounds__(kBuildBlock) k_build_material(Mesh m, const RegionRun* __restrict__ runs,
-                                                               int nruns, const int2* __restrict__ order,
-                                                               const int32_t* __restrict__ order_off,
-                                                               int norder, int numReg, int cost) {
+// elemRep from the region runs (element order), by binary search.
+__global__ void __launch_bounds__(kBuildBlock) k_build_rep(Mesh m, const RegionRun* __restrict__ runs, int nruns,
+                                                          int numReg, int cost) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m.numElem) return;
     int lo = 0, hi = nruns - 1;  // last run with first <= i
@@ -153,26 +150,38 @@ __global__ void __launch_bounds__(kBuildBlock) k_build_material(Mesh m, const Re
         else hi = mid - 1;
     }
     const_cast<int32_t*>(m.elemRep)[i] = region_rep(runs[lo].reg - 1, numReg, cost);
-    lo = 0;
-    hi = norder - 1;  // last range with offset <= i
+}
+
+// An element order from (first, count) ranges with prefix offsets, by
+// binary search over the offsets.
+__global__ void __launch_bounds__(kBuildBlock) k_build_order(int32_t* __restrict__ out, int numElem,
+                                                            const int2* __restrict__ ranges,
+                                                            const int32_t* __restrict__ off, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= numElem) return;
+    int lo = 0, hi = n - 1;  // last range with offset <= t
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (order_off[mid] <= i) lo = mid;
+        if (off[mid] <= t) lo = mid;
         else hi = mid - 1;
     }
-    const_cast<int32_t*>(m.matOrder)[i] = order[lo].x + (i - order_off[lo]);
+    out[t] = ranges[lo].x + (t - off[lo]);
 }
 
 }  // namespace
 
-int launch_build(const Mesh& m, int s, double einit, const RegionRun* runs, int nruns, const int2* order,
-                 const int32_t* order_off, int norder, int numReg, int cost, cudaStream_t st) {
+int launch_build(const Mesh& m, int s, double einit, const RegionRun* runs, int nruns, int numReg, int cost,
+                 cudaStream_t st) {
     k_build_nodes<<<blocks_for(m.numNode, kBuildBlock), kBuildBlock, 0, st>>>(m, s);
     k_build_elems<<<blocks_for(m.numElem, kBuildBlock), kBuildBlock, 0, st>>>(m, s, einit);
     k_build_mass<<<blocks_for(m.numNode, kBuildBlock), kBuildBlock, 0, st>>>(m, s);
-    k_build_material<<<blocks_for(m.numElem, kBuildBlock), kBuildBlock, 0, st>>>(m, runs, nruns, order, order_off,
-                                                                                 norder, numReg, cost);
+    k_build_rep<<<blocks_for(m.numElem, kBuildBlock), kBuildBlock, 0, st>>>(m, runs, nruns, numReg, cost);
     return 4;
+}
+
+int launch_build_order(int32_t* out, int numElem, const int2* ranges, const int32_t* off, int n, cudaStream_t st) {
+    k_build_order<<<blocks_for(numElem, kBuildBlock), kBuildBlock, 0, st>>>(out, numElem, ranges, off, n);
+    return 1;
 }
 
 }  // namespace lulesh

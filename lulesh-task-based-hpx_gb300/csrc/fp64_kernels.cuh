@@ -204,10 +204,12 @@ __device__ __forceinline__ void material_elem(const Mesh& m, int t, double& dtc,
 
 // --- single-problem kernels -------------------------------------------------
 
-__global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m) {
+// all elements, or (RANGED) elements [first, end)
+template <bool RANGED>
+__global__ void __launch_bounds__(kForceBlock) k_forces(Mesh m, int first, int end) {
     if (m.dtime && !m.dtime->active) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m.numElem) forces_elem(m, i);
+    const int i = (RANGED ? first : 0) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < (RANGED ? end : m.numElem)) forces_elem(m, i);
 }
 
 __global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
@@ -230,16 +232,21 @@ __global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
 
 // Elements visited in repeat-count order so a warp's lanes run the same
 // number of EOS passes; the dt minima end in a last-block reduction.
-__global__ void __launch_bounds__(kMatBlock) k_material(Mesh m) {
+__global__ void __launch_bounds__(kMatBlock) k_material(Mesh m, int first, int end, int accumulate) {
     if (m.dtime && !m.dtime->active) return;
     double dtc = 1.0e+20, dth = 1.0e+20;  // lulesh.cc:2214-2215
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.numElem; t += gridDim.x * blockDim.x)
+    for (int t = first + blockIdx.x * blockDim.x + threadIdx.x; t < end; t += gridDim.x * blockDim.x)
         material_elem(m, t, dtc, dth);
-    finish_dt_reduction(m, dtc, dth);
+    finish_dt_reduction(m, dtc, dth, accumulate != 0);
 }
 
 int launch_forces(const Mesh& m, cudaStream_t s) {
-    k_forces<<<blocks_for(m.numElem, kForceBlock), kForceBlock, 0, s>>>(m);
+    k_forces<false><<<blocks_for(m.numElem, kForceBlock), kForceBlock, 0, s>>>(m, 0, m.numElem);
+    return 1;
+}
+int launch_forces_range(const Mesh& m, int first, int end, cudaStream_t s) {
+    if (end <= first) return 0;
+    k_forces<true><<<blocks_for(end - first, kForceBlock), kForceBlock, 0, s>>>(m, first, end);
     return 1;
 }
 int launch_nodes(const Mesh& m, double dt, cudaStream_t s) {
@@ -251,7 +258,11 @@ int launch_kinematics(const Mesh& m, double dt, cudaStream_t s) {
     return 1;
 }
 int launch_material(const Mesh& m, cudaStream_t s) {
-    k_material<<<m.matGrid, kMatBlock, 0, s>>>(m);
+    k_material<<<m.matGrid, kMatBlock, 0, s>>>(m, 0, m.numElem, 0);
+    return 1;
+}
+int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s) {
+    k_material<<<m.matGrid, kMatBlock, 0, s>>>(m, first, end, accumulate ? 1 : 0);
     return 1;
 }
 

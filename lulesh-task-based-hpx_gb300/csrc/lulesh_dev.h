@@ -106,22 +106,32 @@ inline int blocks_for(int n, int b) { return (n + b - 1) / b; }
 // kernels it launched. `dt` is used unless m.dtime is set.
 namespace fp64 {
 int launch_forces(const Mesh& m, cudaStream_t s);
+int launch_forces_range(const Mesh& m, int first, int end, cudaStream_t s);  // elements [first, end)
 int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
 int launch_material(const Mesh& m, cudaStream_t s);
+// matOrder positions [first, end); accumulate: fold the dt minima into m.result's
+int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
 }  // namespace fp64
 namespace fp64x {
 int launch_forces(const Mesh& m, cudaStream_t s);
+int launch_forces_range(const Mesh& m, int first, int end, cudaStream_t s);  // elements [first, end)
 int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
 int launch_material(const Mesh& m, cudaStream_t s);
+// matOrder positions [first, end); accumulate: fold the dt minima into m.result's
+int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
 }  // namespace fp64x
 namespace mixed {
 int launch_forces(const Mesh& m, cudaStream_t s);
+int launch_forces_range(const Mesh& m, int first, int end, cudaStream_t s);  // elements [first, end)
 int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
 int launch_material(const Mesh& m, cudaStream_t s);
+// matOrder positions [first, end); accumulate: fold the dt minima into m.result's
+int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
 int launch_mirror(const Mesh& m, cudaStream_t s);
+int launch_mirror_range(const Mesh& m, int first, int end, cudaStream_t s);  // nodes [first, end)
 }  // namespace mixed
 
 // Device-side TimeIncrement for the graph form (time_increment.cu).
@@ -207,13 +217,13 @@ void default_params(lulesh_params& P);
 void initial_time_state(int s, double energy_scale, lulesh_time_state& ts, double& einit);
 
 // Device build of the initial state of problem s (device_init.cu): every
-// array of a carved mesh from the analytic cube, the region runs expanded
-// into elemRep and matOrder. `runs` are in element order, `order` lists
-// (first, count) element ranges in matOrder order with prefix offsets
-// `order_off` (norder + 1 entries); all three in device memory.
-int launch_build(const Mesh& m, int s, double einit, const RegionRun* runs, int nruns,
-                 const int2* order, const int32_t* order_off, int norder, int numReg, int cost,
+// array of a carved mesh from the analytic cube but matOrder, the region
+// runs (element order, device memory) expanded into elemRep.
+int launch_build(const Mesh& m, int s, double einit, const RegionRun* runs, int nruns, int numReg, int cost,
                  cudaStream_t st);
+// Expands (first, count) element ranges with prefix offsets `off` (n + 1
+// entries, device memory) into an element order out[numElem].
+int launch_build_order(int32_t* out, int numElem, const int2* ranges, const int32_t* off, int n, cudaStream_t st);
 
 // Handle-independent instance set-up shared by the single-problem handle and
 // the batch pool (capi.cu).
@@ -227,9 +237,12 @@ int mesh_init(Mesh& m, char* base, const lulesh_domain_view* v, int precision, c
 int check_problem(const lulesh_problem* p);
 // Builds problem p on the device into an already carved mesh with numElem
 // and numNode set (the build kernels, then a wait); fills *ts and, when
-// given, *classes as mesh_init_problem does.
+// given, *classes as mesh_init_problem does. With slab_order and slabs > 1
+// it also writes the material order split into that many slabs of whole
+// element planes (repeat-count order within a slab) to slab_order[N_e],
+// for a material phase run slab by slab.
 int mesh_fill_problem(Mesh& m, const lulesh_problem* p, int precision, cudaStream_t s, lulesh_time_state* ts,
-                      std::vector<int2>* classes);
+                      std::vector<int2>* classes, int slabs, int32_t* slab_order);
 // The same for problem p built on the device (no host Domain): fills *ts
 // with the problem's initial time state and *classes with (repeat count,
 // elements) pairs, largest repeat count first; waits for the build.

@@ -1065,9 +1065,11 @@ __device__ __forceinline__ void block_min2(double& a, double& b) {
 }
 
 // Publishes this block's (dtc, dth) minima; the last block to arrive reduces
-// all partials into m.result and re-arms the counter. One pass, no second
-// launch. Every thread of the block must call it.
-__device__ __forceinline__ void finish_dt_reduction(const Mesh& m, double dtc, double dth) {
+// all partials into m.result (with accumulate, into the minima already
+// there: a launch over part of the elements) and re-arms the counter. One
+// pass, no second launch. Every thread of the block must call it.
+__device__ __forceinline__ void finish_dt_reduction(const Mesh& m, double dtc, double dth,
+                                                    bool accumulate = false) {
     block_min2(dtc, dth);
     __shared__ bool last;
     if (threadIdx.x == 0) {
@@ -1088,8 +1090,8 @@ __device__ __forceinline__ void finish_dt_reduction(const Mesh& m, double dtc, d
     __syncthreads();  // block_min2's shared scratch is reused
     block_min2(a, b);
     if (threadIdx.x == 0) {
-        m.result->dtcourant = a;
-        m.result->dthydro = b;
+        m.result->dtcourant = accumulate ? fmin(a, m.result->dtcourant) : a;
+        m.result->dthydro = accumulate ? fmin(b, m.result->dthydro) : b;
         m.result->blocks_done = 0u;
     }
 }
