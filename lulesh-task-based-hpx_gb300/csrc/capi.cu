@@ -380,6 +380,9 @@ int new_handle(int32_t precision, int ne, int nn, lulesh_dev** out) {
     if (!d) return LULESH_ENOMEM;
     d->precision = precision;
     d->L = launchers_for(precision);
+    // 8 material blocks per SM: with the elements in repeat-count order this
+    // balanced the grid-stride loop best in a sweep of 5 to 28 per SM, for
+    // both the double and the mixed kernel (1.6 waves for the latter)
     const int matGrid = std::max(1, std::min(lulesh::blocks_for(ne, lulesh::kMatBlock), sms * 8));
     Arena measure;
     layout(d, measure, ne, nn, matGrid);
