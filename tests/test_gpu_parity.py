@@ -76,6 +76,29 @@ def test_exact_path_full_run_bitwise(lulesh, oracle_mod):
     _assert_fields_equal(dom, o)
 
 
+TINY = [(1, 11, 1, 1), (1, 1, 1, 1), (2, 11, 1, 1), (3, 11, 1, 1), (3, 21, 2, 2), (4, 1, 0, 0), (5, 16, 1, 3)]
+
+
+@pytest.mark.parametrize("problem", TINY, ids=[f"s{p[0]}r{p[1]}b{p[2]}c{p[3]}" for p in TINY])
+def test_tiny_meshes_to_stoptime(lulesh, oracle_mod, problem):
+    """Edge sizes down to one element (s=1 reaches stoptime in one step with
+    dt = 1e-2), single-region problems, balance 0 and cost 0: the exact
+    variant equals the oracle bit for bit, the fast and mixed variants land
+    within their bars, every variant with the oracle's cycle count."""
+    s, r, b, c = problem
+    o = oracle_mod.Oracle(s, r, b, c, threads=1, portable_cbrt=True)
+    assert o.run() == 0
+    dom, dev, n = _run_device(lulesh, s, r, b, c, "fp64_exact")
+    assert n == o.cycle
+    _assert_fields_equal(dom, o)
+    assert dom.time_state.time == o.scalar("time") and dom.time_state.deltatime == o.scalar("deltatime")
+    e0 = float(o.field("e")[0])
+    for precision, tol in (("fp64", E0_TOL_FP64), ("mixed", E0_TOL_MIXED)):
+        d2, _, n2 = _run_device(lulesh, s, r, b, c, precision)
+        assert n2 == o.cycle, precision
+        assert abs(d2.e[0] - e0) <= tol * abs(e0), precision
+
+
 @pytest.mark.parametrize("s", [8, 10, 16, 20, 30, 45])
 def test_fp64_full_run_vs_reference(lulesh, golden_results, s):
     g = _golden(golden_results, s)

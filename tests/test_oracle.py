@@ -75,7 +75,10 @@ def test_thread_count_does_not_change_bits(oracle_mod):
         np.testing.assert_array_equal(runs[0][f], runs[1][f], err_msg=f)
 
 
-REF_CASES = [(7, 11, 1, 1, 40), (13, 16, 2, 3, 25), (6, 5, 0, 0, 60)]
+# the last three run to stoptime (--i above their cycle counts): one element
+# (one step), two and three elements a side
+REF_CASES = [(7, 11, 1, 1, 40), (13, 16, 2, 3, 25), (6, 5, 0, 0, 60), (1, 11, 1, 1, 10), (2, 1, 1, 1, 10),
+             (3, 21, 2, 2, 100)]
 
 
 @pytest.mark.skipif(not Path("/root/reference/lulesh.cc").exists(),
