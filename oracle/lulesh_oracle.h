@@ -2,10 +2,10 @@
  *
  * A plain-C restatement of the reference algorithm of
  * esa-tu-darmstadt/lulesh-task-based-hpx (lulesh.cc, lulesh-init.cc,
- * lulesh-util.cc). It is the checker for the GPU path and the timed CPU
- * baseline on machines where the reference sources are absent. Built with
- * -ffp-contract=off it reproduces the reference, compiled the same way, bit
- * for bit (tests/test_oracle_vs_reference.py pins this).
+ * lulesh-util.cc). It is the oracle the GPU path's results are compared
+ * with, and the timed CPU baseline where the reference sources are absent.
+ * Built with -ffp-contract=off it reproduces the reference, compiled the
+ * same way, bit for bit (tests/test_oracle.py pins this).
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use it.
  */

@@ -2,9 +2,10 @@
 
 The oracle is a C restatement of the reference algorithm
 (esa-tu-darmstadt/lulesh-task-based-hpx lulesh.cc / lulesh-init.cc), checked
-bit for bit against the reference's own sources (tests/test_oracle_vs_reference.py
-and the golden fixtures in tests/golden/). Only tests/, __graft_entry__.smoke()
-and bench.py's CPU baseline use it, as the checker; the GPU product never does.
+bit for bit against the reference's own sources (tests/test_oracle.py and the
+golden fixtures in tests/golden/). Only tests/, __graft_entry__.smoke() and
+bench.py's CPU baseline use it, to compare results with; the GPU product never
+does.
 """
 from __future__ import annotations
 

@@ -113,7 +113,7 @@ def test_fp64_full_run_vs_reference(lulesh, golden_results, s):
 
 
 def test_fp64_s90_1000_cycles_vs_reference(lulesh, golden_results):
-    """The survey's GPU FP64 configuration: --s 90 --r 11 --i 1000."""
+    """The GPU double configuration --s 90 --r 11 --i 1000 (729,000 elements)."""
     g = _golden(golden_results, 90, its=1000)
     dom, dev, n = _run_device(lulesh, 90, 11, 1, 1, "fp64", its=1000)
     assert n == dom.cycle == g["cycles"] == 1000
@@ -143,7 +143,7 @@ def test_device_final_report_equals_host(lulesh, golden_results, precision):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_s150_r21_to_stoptime_vs_oracle(lulesh, precision):
-    """The spec configuration run whole: s=150 r=21 (3,375,000
+    """The headline configuration run whole: s=150 r=21 (3,375,000
     elements) to stoptime through the CUDA-graph time loop, against the CPU
     oracle's run (tests/golden/s150_r21.json): same cycle count; e(0) within
     1e-10 (double) or 1e-6 (mixed); double symmetry diffs at the reference's

@@ -63,7 +63,7 @@ def test_rank_setup_barrier_and_max_over_ranks(tmp_path):
 
 
 def test_reference_arm_prints_once_under_torchrun():
-    """The driver's own launch line with N=2: rank 0 times the reference's
+    """torchrun's launch line with N=2: rank 0 times the reference's
     CPU path and prints one JSON line; rank 1 exits 0 without work."""
     _cpu_only()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",

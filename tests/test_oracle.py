@@ -14,6 +14,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import oracle  # noqa: E402  (on sys.path through conftest)
 from conftest import golden_dump
 
 FAST_RUNS = [(8, 11, 1, 1), (10, 11, 1, 1), (12, 21, 1, 1), (12, 1, 1, 1), (9, 16, 2, 2),
@@ -81,7 +82,7 @@ REF_CASES = [(7, 11, 1, 1, 40), (13, 16, 2, 3, 25), (6, 5, 0, 0, 60), (1, 11, 1,
              (3, 21, 2, 2, 100)]
 
 
-@pytest.mark.skipif(not Path("/root/reference/lulesh.cc").exists(),
+@pytest.mark.skipif(not (oracle.REF_SOURCES / "lulesh.cc").exists(),
                     reason="reference sources not present on this machine")
 @pytest.mark.parametrize("s,r,b,c,its", REF_CASES)
 def test_oracle_equals_reference_binary(oracle_mod, tmp_path, s, r, b, c, its):
