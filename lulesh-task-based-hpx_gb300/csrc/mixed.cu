@@ -34,9 +34,46 @@ __device__ __forceinline__ void rel8(const float2* __restrict__ p, const int nl[
     for (int k = 0; k < 8; ++k) r[k] = (a[k].x - a[0].x) + (a[k].y - a[0].y);
 }
 
+// The float-pair mirror of v, (hi, lo) = (fl(v), fl(v - hi)) with fl the
+// round-to-nearest-even conversion, computed on the integer pipe
+// (conversions between float and double occupy the FP64 pipe): rounding
+// the double's bit pattern to 24 significant bits (add half a unit of the
+// 29 dropped bits, or just under half when the kept last bit is even, then
+// clear them; a carry moves into the exponent as rounding does) gives
+// fl(v) exactly, and v - hi is one exact double subtraction. Bit for bit the
+// conversions' result for |v| in [2^-74, float's largest]; zeros map to
+// zeros and other values take the conversion instructions.
+__device__ __forceinline__ unsigned long long round_to_float_bits(unsigned long long b) {
+    return (b + 0x0FFFFFFFull + ((b >> 29) & 1ull)) & ~((1ull << 29) - 1ull);
+}
+__device__ __forceinline__ float float_from_rounded(unsigned long long b) {
+    const unsigned e = unsigned(b >> 52) & 0x7ffu;
+    return __uint_as_float((unsigned(b >> 32) & 0x80000000u) | ((e - 896u) << 23) |
+                           (unsigned(b >> 29) & 0x7fffffu));
+}
+
 __device__ __forceinline__ float2 split(double v) {
-    const float hi = __double2float_rn(v);
-    return make_float2(hi, __double2float_rn(v - double(hi)));
+    const unsigned long long b = __double_as_longlong(v);
+    const unsigned e = unsigned(b >> 52) & 0x7ffu;
+    if ((b << 1) == 0ull) return make_float2(__uint_as_float(unsigned(b >> 32)), 0.0f);  // +-0
+    if (e < 949u || e > 1150u) {
+        const float hi = __double2float_rn(v);
+        return make_float2(hi, __double2float_rn(v - double(hi)));
+    }
+    const unsigned long long hb = round_to_float_bits(b);
+    const unsigned long long lb = __double_as_longlong(v - __longlong_as_double(hb));
+    return make_float2(float_from_rounded(hb), (lb << 1) == 0ull ? 0.0f : float_from_rounded(round_to_float_bits(lb)));
+}
+
+// float -> double, exact, on the integer pipe for zeros and normal floats.
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if ((u << 1) == 0u) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(u) << 32));
+    if (e == 0u || e == 0xffu) return double(f);
+    return __longlong_as_double(static_cast<long long>(
+        (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
+        (static_cast<unsigned long long>(e + 896u) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));
 }
 
 __device__ __forceinline__ void mirror_node(const Mesh& m, int n) {
@@ -112,7 +149,7 @@ struct Neumaier {
         else c += (v - t) + s;
         s = t;
     }
-    __device__ __forceinline__ double value() const { return double(s) + double(c); }
+    __device__ __forceinline__ double value() const { return widen(s) + widen(c); }
 };
 
 __device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt) {
