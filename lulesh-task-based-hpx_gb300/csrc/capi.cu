@@ -195,7 +195,9 @@ void carve_mesh(Mesh& m, Arena& a, int precision, int ne, int nn) {
 void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     Mesh& m = d->m;
     carve_mesh(m, a, d->precision, ne, nn);
-    m.partials = a.take<lulesh::DtPartial>(matGrid);
+    // one partial per block of the material launch: the full grid, or a
+    // slab launch of lulesh_leapfrog with one thread per element
+    m.partials = a.take<lulesh::DtPartial>(std::max(matGrid, lulesh::blocks_for(ne, lulesh::kMatBlock)));
     m.result = a.take<StepResult>(1);
     d->d_time = a.take<DevTime>(1);
     d->d_verify = a.take<double>(4);
@@ -628,6 +630,9 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     Mesh ms = m;  // the slab-major material order: positions [e_lo, e_hi) are the slab's elements
     if (slabs > 1) ms.matOrder = d->matOrderSlab;
     for (int sl = 0; sl < slabs; ++sl) {
+        // one thread per element: blocks schedule dynamically, the slab's
+        // most expensive elements first (repeat-count order within a slab)
+        ms.matGrid = std::max(1, lulesh::blocks_for(int(e_hi[sl] - e_lo[sl]), lulesh::kMatBlock));
         d->launches += d->L.material_range(ms, int(e_lo[sl]), int(e_hi[sl]), sl > 0, d->stream);
         CK(cudaEventRecord(d->ev_mat[sl], d->stream));
         CK(cudaStreamWaitEvent(d->mstream, d->ev_mat[sl], 0));
