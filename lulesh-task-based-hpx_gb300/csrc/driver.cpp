@@ -41,15 +41,23 @@ int main(int argc, char** argv) {
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
         if (a.rfind("--hpx:", 0) == 0) continue;
+        // --name=value, which the reference's option parser accepts too
+        std::string inline_value;
+        bool has_inline = false;
+        if (const size_t eq = a.find('='); eq != std::string::npos && a.rfind("--", 0) == 0) {
+            inline_value = a.substr(eq + 1);
+            a = a.substr(0, eq);
+            has_inline = true;
+        }
         if (a == "--q") { quiet = 1; continue; }
         if (a == "--p") { prog = 1; continue; }
         if (a == "--v") continue;
         if (a == "--graph") { graph = 1; continue; }
-        if (i + 1 >= argc) {
+        if (!has_inline && i + 1 >= argc) {
             std::fprintf(stderr, "option %s needs a value\n", a.c_str());
             return 2;
         }
-        std::string v = argv[++i];
+        std::string v = has_inline ? inline_value : std::string(argv[++i]);
         if (a == "--s") nx = std::atoi(v.c_str());
         else if (a == "--r") nr = std::atoi(v.c_str());
         else if (a == "--i") its = std::atoi(v.c_str());

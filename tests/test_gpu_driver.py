@@ -39,6 +39,17 @@ def test_quiet_prints_the_reference_csv_line(lulesh, golden_results):
     assert e0.strip() == f"{float(g['e0']):.6e}"
 
 
+def test_equals_form_and_ignored_flags(lulesh, golden_results):
+    """--name=value as the reference's option parser takes it, and the
+    reference's viz and HPX task-size flags accepted (no effect here)."""
+    g = _golden(golden_results, 12, r=21)
+    out = subprocess.run([str(EXE), "--s=12", "--r=21", "--q", "--f", "2", "--v", "--elems-per-task=64",
+                          "--task-size", "4", "--hpx:threads=2"],
+                         capture_output=True, text=True, check=True).stdout.strip()
+    s, r, cycles = out.split(",")[:3]
+    assert (s, r, cycles) == ("12", "21", str(g["cycles"]))
+
+
 def test_iteration_cap(lulesh):
     out = subprocess.run([str(EXE), "--s", "10", "--i", "37", "--q"], capture_output=True, text=True,
                          check=True).stdout
