@@ -419,7 +419,7 @@ def run_batched(lul, precision: str, n: int, seed: int, tune: bool) -> dict:
     for sp in specs:
         b.admit(**sp)
     admit_s = time.perf_counter() - t0
-    tuning = b.autotune(cycles=1) if tune else b.tuning()
+    tuning = b.autotune(cycles=3) if tune else b.tuning()
     launches0 = b.launches
     total_ms, rounds = 0.0, 0
     while True:

@@ -225,10 +225,12 @@ typedef struct lulesh_slot_status {
 } lulesh_slot_status;
 
 /* Per-phase launch shapes of the persistent kernels (forces, nodes,
- * kinematics, material) and the tile size in units. */
+ * kinematics, material), the tiles a block takes per queue access, and the
+ * tile size in units. */
 typedef struct lulesh_batch_tuning {
     int32_t block[4];
     int32_t blocks_per_sm[4];
+    int32_t grab[4]; /* tiles a block takes per queue access (1..64) */
     int32_t tile;
     int32_t pad_;
     double ms_per_cycle; /* measured by lulesh_batch_autotune */

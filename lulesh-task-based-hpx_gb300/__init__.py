@@ -80,8 +80,8 @@ class SlotStatus(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("block", C.c_int32 * 4), ("blocks_per_sm", C.c_int32 * 4), ("tile", C.c_int32),
-                ("pad_", C.c_int32), ("ms_per_cycle", C.c_double)]
+    _fields_ = [("block", C.c_int32 * 4), ("blocks_per_sm", C.c_int32 * 4), ("grab", C.c_int32 * 4),
+                ("tile", C.c_int32), ("pad_", C.c_int32), ("ms_per_cycle", C.c_double)]
 
 
 class Request(C.Structure):
@@ -437,8 +437,8 @@ def serve(requests: list[dict], precision: str = "mixed", hbm_budget: int = 160 
 
 
 def _tuning_dict(t: BatchTuning) -> dict:
-    return {"block": list(t.block), "blocks_per_sm": list(t.blocks_per_sm), "tile": t.tile,
-            "ms_per_cycle": t.ms_per_cycle}
+    return {"block": list(t.block), "blocks_per_sm": list(t.blocks_per_sm), "grab": list(t.grab),
+            "tile": t.tile, "ms_per_cycle": t.ms_per_cycle}
 
 
 class Batch:
@@ -529,8 +529,9 @@ class Batch:
         _check(self._lib.lulesh_batch_get_tuning(self._h, C.byref(t)), "lulesh_batch_get_tuning")
         return _tuning_dict(t)
 
-    def set_tuning(self, block, blocks_per_sm, tile: int) -> None:
-        t = BatchTuning((C.c_int32 * 4)(*block), (C.c_int32 * 4)(*blocks_per_sm), tile, 0, 0.0)
+    def set_tuning(self, block, blocks_per_sm, tile: int, grab=(1, 1, 1, 1)) -> None:
+        t = BatchTuning((C.c_int32 * 4)(*block), (C.c_int32 * 4)(*blocks_per_sm), (C.c_int32 * 4)(*grab),
+                        tile, 0, 0.0)
         _check(self._lib.lulesh_batch_set_tuning(self._h, C.byref(t)), "lulesh_batch_set_tuning")
 
     @property

@@ -226,7 +226,7 @@ BatchLaunch shape(const lulesh_batch* b, int phase) {
     const int block = b->tuning.block[phase];
     const int occ = std::max(1, b->L.occupancy(phase, block));
     const int per_sm = std::max(1, std::min(b->tuning.blocks_per_sm[phase], occ));
-    return {block, b->sms * per_sm};
+    return {block, b->sms * per_sm, std::max(1, b->tuning.grab[phase])};
 }
 
 // Rebuilds the three tile tables from the slots in use. Returns true when a
@@ -434,6 +434,7 @@ int lulesh_batch_create(int32_t precision, uint64_t pool_bytes, int32_t max_slot
     for (int p = 0; p < 4; ++p) {
         b->tuning.block[p] = blocks[p];
         b->tuning.blocks_per_sm[p] = 8;
+        b->tuning.grab[p] = 1;
     }
     b->tuning.tile = 1024;
     *out = b;
@@ -584,7 +585,8 @@ int lulesh_batch_get_tuning(const lulesh_batch* b, lulesh_batch_tuning* out) {
 int lulesh_batch_set_tuning(lulesh_batch* b, const lulesh_batch_tuning* t) {
     if (!b || !t || t->tile < 32) return LULESH_EINVAL;
     for (int p = 0; p < 4; ++p)
-        if (t->block[p] < 32 || t->block[p] > lulesh::kBatchMaxBlock || t->block[p] % 32 || t->blocks_per_sm[p] < 1)
+        if (t->block[p] < 32 || t->block[p] > lulesh::kBatchMaxBlock || t->block[p] % 32 || t->blocks_per_sm[p] < 1 ||
+            t->grab[p] < 1 || t->grab[p] > 64)
             return LULESH_EINVAL;
     BCK(cudaStreamSynchronize(b->stream));
     b->tuning = *t;
@@ -675,6 +677,20 @@ extern "C" int lulesh_batch_autotune(lulesh_batch* b, int32_t cycles, lulesh_bat
                     best = t;
                 }
             }
+    // per-phase tiles per queue access (fewer queue round trips for cheap tiles)
+    const int grabs[4] = {1, 2, 4, 8};
+    for (int p = 0; p < 4 && st == LULESH_OK; ++p)
+        for (int gi = 0; gi < 4 && st == LULESH_OK; ++gi) {
+            lulesh_batch_tuning t = best;
+            t.grab[p] = grabs[gi];
+            if (t.grab[p] == best.grab[p]) continue;
+            double ms = 0;
+            st = measure(t, &ms);
+            if (st == LULESH_OK && ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        }
     best.ms_per_cycle = best_ms / cycles;
     const int st2 = copy_state(false);
     cudaFree(snap);

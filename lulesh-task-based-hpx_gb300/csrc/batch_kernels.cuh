@@ -8,8 +8,10 @@
 // 20 EOS passes, share the SMs without a launch per instance. Material tiles
 // are queued most expensive first.
 //
-// A block copies the tile's Mesh (device pointers of that instance) into
-// shared memory and runs the variant's per-element function over the tile.
+// A block takes `grab` consecutive tiles per queue access (fetching the next
+// position while they run), copies a tile's Mesh (device pointers of that
+// instance) into shared memory when the instance changes, and runs the
+// variant's per-element function over the tile.
 // Each instance keeps its own dt (DevTime), and the material phase lowers
 // the instance's Courant/hydro minima with atomic minima on the doubles' bit
 // patterns (exact for positive values, so the order does not matter).
@@ -25,7 +27,7 @@ __device__ __forceinline__ void atomic_min_pos(double* addr, double v) {
 }
 
 template <int PHASE>
-__global__ void __launch_bounds__(kBatchMaxBlock) kb_phase(BatchCtl c) {
+__global__ void __launch_bounds__(kBatchMaxBlock) kb_phase(BatchCtl c, int grab) {
     constexpr int kind = (PHASE == 1) ? TILES_NODE : (PHASE == 3) ? TILES_MAT : TILES_ELEM;
     __shared__ __align__(16) unsigned long long s_mesh[(sizeof(Mesh) + 7) / 8];
     __shared__ int s_tile;
@@ -34,20 +36,29 @@ __global__ void __launch_bounds__(kBatchMaxBlock) kb_phase(BatchCtl c) {
     const Mesh& m = *reinterpret_cast<const Mesh*>(s_mesh);
     const int ntiles = __ldg(c.ntiles + kind);
     const BatchTile* tiles = c.tiles[kind];
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&c.queue[PHASE], 1u);
-        __syncthreads();
-        const int t = s_tile;
-        if (t >= ntiles) break;
-        const BatchTile tile = tiles[t];
-        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(c.meshes + tile.inst);
-        for (int k = threadIdx.x; k < (int)((sizeof(Mesh) + 7) / 8); k += blockDim.x) s_mesh[k] = src[k];
-        if (threadIdx.x == 0) {
-            s_active = c.times[tile.inst].active;
-            s_dt = c.times[tile.inst].deltatime;
-        }
-        __syncthreads();
-        if (s_active) {
+    int cur_inst = -1;
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(&c.queue[PHASE], (unsigned)grab);
+    __syncthreads();
+    int t0 = s_tile;
+    while (t0 < ntiles) {
+        const int t1 = min(t0 + grab, ntiles);
+        __syncthreads();  // every thread has read s_tile
+        // the next queue position, fetched while this grab's tiles run
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(&c.queue[PHASE], (unsigned)grab);
+        for (int t = t0; t < t1; ++t) {
+            const BatchTile tile = tiles[t];
+            if (tile.inst != cur_inst) {  // the same for every thread of the block
+                __syncthreads();          // the previous instance's Mesh is no longer read
+                const unsigned long long* src = reinterpret_cast<const unsigned long long*>(c.meshes + tile.inst);
+                for (int k = threadIdx.x; k < (int)((sizeof(Mesh) + 7) / 8); k += blockDim.x) s_mesh[k] = src[k];
+                if (threadIdx.x == 0) {
+                    s_active = c.times[tile.inst].active;
+                    s_dt = c.times[tile.inst].deltatime;
+                }
+                __syncthreads();
+                cur_inst = tile.inst;
+            }
+            if (!s_active) continue;
             if (PHASE == 3) {
                 double dtc = 1.0e+20, dth = 1.0e+20;
                 for (int k = threadIdx.x; k < tile.count; k += blockDim.x)
@@ -69,16 +80,17 @@ __global__ void __launch_bounds__(kBatchMaxBlock) kb_phase(BatchCtl c) {
                 }
             }
         }
-        __syncthreads();  // the next tile overwrites the shared Mesh
+        __syncthreads();  // thread 0's next queue position is visible
+        t0 = s_tile;
     }
 }
 
 int launch_batch_phase(int phase, const BatchCtl& c, const BatchLaunch& l, cudaStream_t s) {
     switch (phase) {
-        case 0: kb_phase<0><<<l.grid, l.block, 0, s>>>(c); break;
-        case 1: kb_phase<1><<<l.grid, l.block, 0, s>>>(c); break;
-        case 2: kb_phase<2><<<l.grid, l.block, 0, s>>>(c); break;
-        default: kb_phase<3><<<l.grid, l.block, 0, s>>>(c); break;
+        case 0: kb_phase<0><<<l.grid, l.block, 0, s>>>(c, l.grab); break;
+        case 1: kb_phase<1><<<l.grid, l.block, 0, s>>>(c, l.grab); break;
+        case 2: kb_phase<2><<<l.grid, l.block, 0, s>>>(c, l.grab); break;
+        default: kb_phase<3><<<l.grid, l.block, 0, s>>>(c, l.grab); break;
     }
     return 1;
 }

@@ -165,6 +165,7 @@ struct BatchCtl {
 struct BatchLaunch {
     int32_t block;  // threads per block
     int32_t grid;   // persistent blocks
+    int32_t grab;   // tiles taken per queue access
 };
 
 constexpr int kBatchMaxBlock = 256;
