@@ -67,7 +67,7 @@ BYTES_PER_UNIT = {
 # array exceeds L2 (profiles/dram_traffic_s100.md); scaled by units per launch.
 TRAFFIC_PER_UNIT = {
     "fp64": {"forces": 271, "nodes": 342, "kinematics": 141, "material": 183},
-    "mixed": {"forces": 188, "nodes": 274, "kinematics": 156, "material": 149},
+    "mixed": {"forces": 188, "nodes": 275, "kinematics": 156, "material": 149},
 }
 # FP64-pipe instructions per unit (thread level: sm__inst_executed_pipe_fp64
 # x 32 / units) measured by ncu at s=100 for the branch-free kernels; the
@@ -75,7 +75,7 @@ TRAFFIC_PER_UNIT = {
 # elements), so it has none here.
 FP64_INSTR_PER_UNIT = {
     "fp64": {"forces": 726.0, "nodes": 35.7, "kinematics": 337.0},
-    "mixed": {"forces": 8.0, "nodes": 45.0, "kinematics": 95.0},
+    "mixed": {"forces": 8.0, "nodes": 38.9, "kinematics": 95.0},
 }
 # Double-precision operations per unit of the reference's formulation (adds,
 # multiplies, divides, square and cube roots each counted once), from
