@@ -165,7 +165,7 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     gather8(m.y, nl, y);
     gather8(m.z, nl, z);
     const double volume = hex_volume(x, y, z);
-    const double relv = quot(volume, LD(m.volo + i));
+    const double relv = quot_refined(volume, LD(m.volo + i));
     const double vold = m.v[i];
     m.vnew[i] = relv;
     m.delv[i] = relv - vold;

@@ -178,7 +178,7 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
         gather8(m.z, nl, zd8);
         volume = hex_volume(xd8, yd8, zd8);  // double: relative volume and delv need it
     }
-    const double relv = quot(volume, LD(m.volo + i));
+    const double relv = quot_refined(volume, LD(m.volo + i));
     const double vold = m.v[i];
     m.vnew[i] = relv;
     m.delv[i] = relv - vold;
