@@ -66,7 +66,7 @@ BYTES_PER_UNIT = {
 # DRAM bytes (read + write) per unit measured by ncu at s=100, where every
 # array exceeds L2 (profiles/dram_traffic_s100.md); scaled by units per launch.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"forces": 271, "nodes": 342, "kinematics": 141, "material": 183},
+    "fp64": {"forces": 272, "nodes": 342, "kinematics": 142, "material": 183},
     "mixed": {"forces": 188, "nodes": 275, "kinematics": 156, "material": 149},
 }
 # FP64-pipe instructions per unit (thread level: sm__inst_executed_pipe_fp64
@@ -74,8 +74,8 @@ TRAFFIC_PER_UNIT = {
 # material kernel's count depends on the state (EOS repeats, compressing
 # elements), so it has none here.
 FP64_INSTR_PER_UNIT = {
-    "fp64": {"forces": 726.0, "nodes": 35.7, "kinematics": 337.0},
-    "mixed": {"forces": 8.0, "nodes": 38.9, "kinematics": 95.0},
+    "fp64": {"forces": 725.0, "nodes": 35.7, "kinematics": 336.0},
+    "mixed": {"forces": 8.0, "nodes": 38.9, "kinematics": 96.0},
 }
 # Double-precision operations per unit of the reference's formulation (adds,
 # multiplies, divides, square and cube roots each counted once), from
@@ -431,6 +431,7 @@ def run_batched(lul, precision: str, n: int, seed: int, tune: bool) -> dict:
     st = b.status()
     zc = sum(x["numElem"] * x["cycle"] for x in st)
     errs = sum(1 for x in st if x["err"] != 0)
+    launches = b.launches - launches0
     b.close()
     # the same problems run one at a time through the single-problem path
     # (device-built handle, CUDA-graph time loop): device time
@@ -445,7 +446,7 @@ def run_batched(lul, precision: str, n: int, seed: int, tune: bool) -> dict:
            "zone_cycles": zc, "device_s": round(total_ms / 1e3, 3),
            "cycles_min_max": [min(x["cycle"] for x in st), max(x["cycle"] for x in st)],
            "elements": sum(x["numElem"] for x in st), "errors": errs,
-           "gpu_launches": b.launches - launches0, "admit_s": round(admit_s, 2),
+           "gpu_launches": launches, "admit_s": round(admit_s, 2),
            "tuning": tuning,
            "solo_device_s": round(solo_ms / 1e3, 3),
            "vs_solo_runs": round(solo_ms / total_ms, 3),

@@ -389,6 +389,8 @@ class Device:
 
     @property
     def launches(self) -> int:
+        if not self._h:
+            raise RuntimeError("launch count of a closed handle")
         return self._lib.lulesh_dev_launch_count(self._h)
 
     def close(self) -> None:
@@ -536,6 +538,8 @@ class Batch:
 
     @property
     def launches(self) -> int:
+        if not self._h:
+            raise RuntimeError("launch count of a closed handle")
         return self._lib.lulesh_batch_launch_count(self._h)
 
     def close(self) -> None:
