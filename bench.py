@@ -27,8 +27,12 @@ ours (default) prints one JSON line:
                  time to solution and zone-cycles/s
   roofline       dominant kernel vs the measured HBM copy bandwidth, plus its
                  FP64-pipe roof (the bound that actually applies)
+  fom            the reference's report figures for value (and mixed):
+                 grind time in us per zone-cycle and FOM = 1000 / grind
   cpu_baseline   the CPU oracle (a bit-exact restatement of the reference's
-                 code) on this machine's host cores, bounded sample
+                 code) on this machine's host cores, bounded sample (the
+                 reference's reduced s=150 cap of 180 cycles); its sweep
+                 adds the single-thread rate
 reference: the reference's CPU algorithm (the oracle port) on all host cores,
 same workload, same metric.
 
@@ -263,6 +267,14 @@ def time_device(lul, dom, dev, steps: int, world: int, graph: bool = False) -> d
     return prof
 
 
+def fom(value: float) -> dict:
+    """The reference's report figures (lulesh-util.cc:70-112) for a
+    zone-cycles/s rate: grind time = us per zone-cycle, FOM = 1000 / grind
+    (zone-cycles per millisecond; the reference labels it z/s)."""
+    grind = 1e6 / value
+    return {"grind_time_us_per_zone_cycle": float(f"{grind:.6g}"), "fom": float(f"{1e3 / grind:.6g}")}
+
+
 def cpu_oracle_rate(s: int, r: int, cycles: int, threads: int) -> tuple[float, float]:
     import oracle
 
@@ -335,7 +347,7 @@ def run_ours(args) -> None:
         mvalue = world * ne * K / (mprof["max_ms"] / 1e3)
         mixed = {"value": round(mvalue, 1), "unit": UNIT, "dtype": "f32 temporaries + f64 state",
                  "ms_per_step": round(mprof["max_ms"] / K, 4),
-                 "speedup_vs_fp64": round(mvalue / value, 3),
+                 "speedup_vs_fp64": round(mvalue / value, 3), "fom": fom(mvalue),
                  "kernel_ms_per_step": {k: round(v / K, 4) for k, v in mprof["kernel_ms"].items()},
                  "roofline": roofline(mprof, "mixed", ne, nn, rep_avg, fp64_peak, "measured live")}
         mdev.close()
@@ -365,6 +377,12 @@ def run_ours(args) -> None:
         cpu = {"value": round(rate, 1), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{args.cpu_cycles} cycles of s={s} r={r} after 1 warm-up cycle "
                          f"({secs:.1f} s), OpenMP over all host threads"}
+        if args.cpu_cycles_1t > 0:
+            # the reference's thread sweep, its two ends: 1 thread and all cores
+            rate1, secs1 = cpu_oracle_rate(s, r, args.cpu_cycles_1t, 1)
+            cpu["sweep"] = {"threads": [1, threads], "value": [round(rate1, 1), round(rate, 1)],
+                            "sample_1_thread": f"{args.cpu_cycles_1t} cycles of s={s} r={r} after 1 "
+                                               f"warm-up cycle ({secs1:.1f} s)"}
 
     if rank != 0:
         return
@@ -383,6 +401,7 @@ def run_ours(args) -> None:
                 "how": "lulesh_leapfrog per cycle: upload step inputs from pinned host arrays, "
                        "run, download every field the step writes; wall clock"},
         "gpu_launches": launches,
+        "fom": fom(value),
         "kernel_ms_per_step": {k: round(v / K, 4) for k, v in prof["kernel_ms"].items()},
         "roofline": roofline(prof, "fp64", ne, nn, rep_avg, fp64_peak, "measured live"),
         "pipe_rates_per_s": {k: float(f"{v:.4g}") for k, v in rates.items()},
@@ -528,7 +547,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--size", type=int, default=150)
     ap.add_argument("--regions", type=int, default=21)
-    ap.add_argument("--cpu-cycles", type=int, default=120)
+    ap.add_argument("--cpu-cycles", type=int, default=180)
+    ap.add_argument("--cpu-cycles-1t", type=int, default=6)
     ap.add_argument("--skip-mixed", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")

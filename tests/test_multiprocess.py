@@ -108,3 +108,17 @@ def test_roofline_arithmetic():
     # the material kernel has no fixed instruction count: no pipe roof claimed
     prof["kernel_ms"]["material"] = 99.0
     assert bench.roofline(prof, "fp64", ne, nn, 3.26)["fp64_pipe"] is None
+
+
+def test_fom_matches_reference_report_formula():
+    """bench.fom: grind time = elapsed us / cycles / elements and FOM =
+    1000 / grind, as lulesh-util.cc:70-112 prints them (one rank)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    elapsed_s, cycles, elements = 12.5, 932, 27_000
+    rate = elements * cycles / elapsed_s
+    f = bench.fom(rate)
+    grind = elapsed_s * 1e6 / cycles / elements
+    assert f["grind_time_us_per_zone_cycle"] == pytest.approx(grind, rel=1e-5)
+    assert f["fom"] == pytest.approx(1000.0 / grind, rel=1e-5)
