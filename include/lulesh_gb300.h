@@ -371,6 +371,13 @@ int lulesh_domain_pin(lulesh_domain* d, int32_t pin);
  * The double path is bound by out[0]; takes about 50 ms. */
 int lulesh_probe_pipe_rates(double out[5]);
 
+/* Evaluates one arithmetic helper of the fast variants on the device for n
+ * inputs (no counterpart in the reference; accuracy tests compare the results
+ * with correctly rounded host values): fn 0 reciprocal, 1 reciprocal cube
+ * root, 2 square root, 3 reciprocal square root (inputs positive and normal
+ * for 1-3), 4 the hardware seed of the reciprocal. n <= 2^26. */
+int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n);
+
 /* Selects the CUDA device used by handles created afterwards on this thread. */
 int lulesh_set_device(int32_t device);
 

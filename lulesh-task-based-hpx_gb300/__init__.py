@@ -162,6 +162,7 @@ def library() -> C.CDLL:
         "lulesh_domain_pin": (i32, [vp, i32]),
         "lulesh_set_device": (i32, [i32]),
         "lulesh_probe_pipe_rates": (i32, [C.POINTER(dbl)]),
+        "lulesh_probe_math": (i32, [i32, C.POINTER(dbl), C.POINTER(dbl), i64]),
         "lulesh_batch_create": (i32, [i32, C.c_uint64, i32, C.POINTER(vp)]),
         "lulesh_batch_destroy": (None, [vp]),
         "lulesh_batch_footprint": (i32, [i32, i32, C.POINTER(C.c_uint64)]),
@@ -415,6 +416,22 @@ def pipe_rates() -> dict:
     out = (C.c_double * 5)()
     _check(library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
     return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma"), list(out)))
+
+
+MATH_FUNCTIONS = {"rcp": 0, "rcbrt": 1, "sqrt": 2, "rsqrt": 3, "rcp_seed": 4}
+
+
+def probe_math(fn: str, x):
+    """The fast variants' helper `fn` (MATH_FUNCTIONS) evaluated on the
+    device for the doubles x; returns a numpy array."""
+    import numpy as np
+
+    xs = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(xs)
+    _check(library().lulesh_probe_math(MATH_FUNCTIONS[fn], xs.ctypes.data_as(C.POINTER(C.c_double)),
+                                       out.ctypes.data_as(C.POINTER(C.c_double)), xs.size),
+           "lulesh_probe_math")
+    return out
 
 
 def serve(requests: list[dict], precision: str = "mixed", hbm_budget: int = 160 << 30,

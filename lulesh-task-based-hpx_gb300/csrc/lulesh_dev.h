@@ -112,6 +112,8 @@ int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
 int launch_material(const Mesh& m, cudaStream_t s);
 // matOrder positions [first, end); accumulate: fold the dt minima into m.result's
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
+// the fast helpers on n inputs (probe.cu's lulesh_probe_math)
+int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t s);
 }  // namespace fp64
 namespace fp64x {
 int launch_forces(const Mesh& m, cudaStream_t s);

@@ -52,14 +52,20 @@ __device__ __forceinline__ float float_from_rounded(unsigned long long b) {
                            (unsigned(b >> 29) & 0x7fffffu));
 }
 
+// The rare inputs (magnitudes outside the range above) take the conversion
+// instructions in functions of their own: inlined, the compiler evaluates
+// them for every input and selects, and conversions issue on the FP64 pipe.
+__device__ __noinline__ float2 split_convert(double v) {
+    const float hi = __double2float_rn(v);
+    return make_float2(hi, __double2float_rn(v - double(hi)));
+}
+__device__ __noinline__ double widen_convert(float f) { return double(f); }
+
 __device__ __forceinline__ float2 split(double v) {
     const unsigned long long b = __double_as_longlong(v);
     const unsigned e = unsigned(b >> 52) & 0x7ffu;
     if ((b << 1) == 0ull) return make_float2(__uint_as_float(unsigned(b >> 32)), 0.0f);  // +-0
-    if (e < 949u || e > 1150u) {
-        const float hi = __double2float_rn(v);
-        return make_float2(hi, __double2float_rn(v - double(hi)));
-    }
+    if (e < 949u || e > 1150u) return split_convert(v);
     const unsigned long long hb = round_to_float_bits(b);
     const unsigned long long lb = __double_as_longlong(v - __longlong_as_double(hb));
     return make_float2(float_from_rounded(hb), (lb << 1) == 0ull ? 0.0f : float_from_rounded(round_to_float_bits(lb)));
@@ -70,7 +76,7 @@ __device__ __forceinline__ double widen(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xffu;
     if ((u << 1) == 0u) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(u) << 32));
-    if (e == 0u || e == 0xffu) return double(f);
+    if (e == 0u || e == 0xffu) return widen_convert(f);
     return __longlong_as_double(static_cast<long long>(
         (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
         (static_cast<unsigned long long>(e + 896u) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "lulesh_gb300.h"
+#include "lulesh_dev.h"
 
 namespace {
 
@@ -82,5 +83,27 @@ extern "C" int lulesh_probe_pipe_rates(double out[5]) {
     cudaEventDestroy(e1);
     cudaFree(buf);
     if (cudaGetLastError() != cudaSuccess) st = LULESH_ECUDA;
+    return st;
+}
+
+extern "C" int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n) {
+    if (!in || !out || fn < 0 || fn > 4 || n < 1 || n > (int64_t(1) << 26)) return LULESH_EINVAL;
+    const size_t bytes = sizeof(double) * size_t(n);
+    double *d_in = nullptr, *d_out = nullptr;
+    if (cudaMalloc(&d_in, bytes) != cudaSuccess) return LULESH_ENOMEM;
+    if (cudaMalloc(&d_out, bytes) != cudaSuccess) {
+        cudaFree(d_in);
+        return LULESH_ENOMEM;
+    }
+    int st = LULESH_OK;
+    if (cudaMemcpy(d_in, in, bytes, cudaMemcpyHostToDevice) != cudaSuccess) st = LULESH_ECUDA;
+    if (st == LULESH_OK) {
+        lulesh::fp64::launch_math_probe(fn, d_in, d_out, int(n), nullptr);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(out, d_out, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = LULESH_ECUDA;
+    }
+    cudaFree(d_in);
+    cudaFree(d_out);
     return st;
 }

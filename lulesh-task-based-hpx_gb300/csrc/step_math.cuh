@@ -301,6 +301,11 @@ __device__ __forceinline__ double rcbrt_pos(double x) {
     const double r = fma(-x, (y * y) * y, 1.0);
     return fma(y, r * fma(r, 2.0 / 9.0, 1.0 / 3.0), y);
 }
+
+// Square root of a positive normal double in the fast variants: x times the
+// library's reciprocal square root, one rounding more than sqrt (within
+// about one ulp; the probe test measures it) for fewer FP64-pipe slots.
+__device__ __forceinline__ double sqrt_fast(double x) { return x * rsqrt(x); }
 #endif
 
 template <class R>
@@ -879,7 +884,7 @@ __device__ __forceinline__ double ss_guard(double ssc) {
 #if LULESH_EXACT
     return f_le(ssc, .1111111e-36) ? .3333333e-18 : sqrt(ssc);
 #else
-    return f_le(ssc, .1111111e-36) ? .3333333e-18 : ssc * rsqrt(ssc);  // sqrt, one rounding more
+    return f_le(ssc, .1111111e-36) ? .3333333e-18 : sqrt_fast(ssc);
 #endif
 }
 

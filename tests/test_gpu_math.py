@@ -1,0 +1,64 @@
+"""Accuracy of the fast variants' arithmetic helpers on the GPU.
+
+The fast double path replaces the IEEE divide, cube root and square root by
+shorter sequences (step_math.cuh: rcp, rcbrt_pos, sqrt_fast, recip_sqrt).
+lulesh_probe_math evaluates each on the device; the results are compared
+here with the correctly rounded values computed in long double on the host,
+in units in the last place of the double result (ulp). The inputs are seeded
+and span the magnitudes a step can meet (and far beyond).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 1 << 20
+
+
+def _ulp_error(got: np.ndarray, ref: np.ndarray) -> float:
+    spacing = np.spacing(np.abs(ref.astype(np.float64))).astype(np.longdouble)
+    return float((np.abs(got.astype(np.longdouble) - ref) / spacing).max())
+
+
+def _inputs(lo: int, hi: int, negative: bool = False) -> np.ndarray:
+    rng = np.random.default_rng(2024)
+    x = np.ldexp(rng.uniform(1.0, 2.0, N), rng.integers(lo, hi, N))
+    x[:64] = np.ldexp(1.0, np.arange(64) - 32)  # exact powers of two
+    x[64:128] = np.nextafter(np.ldexp(1.0, np.arange(64) - 31), 0.0)  # just below them
+    if negative:
+        x[N // 2:] *= -1.0
+    return x
+
+
+# (helper, exponent range of the inputs, negative inputs too, reference, bound in ulp)
+CASES = [
+    ("rcp", (-100, 100), True, lambda x: 1 / x, 0.55),
+    ("rcbrt", (-100, 100), False, lambda x: 1 / np.cbrt(x), 1.0),
+    ("sqrt", (-1000, 1000), False, np.sqrt, 1.5),
+    ("rsqrt", (-1000, 1000), False, lambda x: 1 / np.sqrt(x), 1.0),
+]
+
+
+@pytest.mark.parametrize("name,span,neg,ref,bound", CASES, ids=[c[0] for c in CASES])
+def test_helper_within_bound(lulesh, name, span, neg, ref, bound):
+    x = _inputs(*span, negative=neg)
+    got = lulesh.probe_math(name, x)
+    err = _ulp_error(got, ref(x.astype(np.longdouble)))
+    assert err <= bound, f"{name}: {err:.3f} ulp"
+
+
+def test_reciprocal_seed_bound(lulesh):
+    """rcp's third-order correction assumes a seed within 2^-19.9 (the
+    truncated series term e^3 is then below 2^-59)."""
+    x = _inputs(-1000, 1000, negative=True)
+    seed = lulesh.probe_math("rcp_seed", x).astype(np.longdouble)
+    ref = 1 / x.astype(np.longdouble)
+    rel = float((np.abs(seed - ref) / np.abs(ref)).max())
+    assert rel <= 2.0 ** -19.9, rel
+
+
+def test_probe_rejects_bad_arguments(lulesh):
+    with pytest.raises(lulesh.LuleshError):
+        lulesh.probe_math("rcp", np.empty(0))
