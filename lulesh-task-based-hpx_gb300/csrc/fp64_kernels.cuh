@@ -196,8 +196,8 @@ __device__ __forceinline__ void material_elem(const Mesh& m, int t, double& dtc,
     m.qq[i] = qq;
     m.ql[i] = ql;
     double vnewc = vnew;
-    if (m.prm.eosvmin != 0.0 && vnewc < m.prm.eosvmin) vnewc = m.prm.eosvmin;
-    if (m.prm.eosvmax != 0.0 && vnewc > m.prm.eosvmax) vnewc = m.prm.eosvmax;
+    if (!f_is_zero(m.prm.eosvmin) && f_lt(vnewc, m.prm.eosvmin)) vnewc = m.prm.eosvmin;
+    if (!f_is_zero(m.prm.eosvmax) && f_gt(vnewc, m.prm.eosvmax)) vnewc = m.prm.eosvmax;
     const double ss = eos_element(m, i, vnewc, LD(m.elemRep + i));
     dt_constraints(m.prm, ss, vdov, LD(m.arealg + i), dtc, dth);
 }

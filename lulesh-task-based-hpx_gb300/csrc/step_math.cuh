@@ -135,6 +135,10 @@ __device__ __forceinline__ void cofactors(const R J[3][3], R c[3][3]) {
 }
 #endif
 
+// zero tests of the compare helpers below (declared here for jacobian_singular)
+__device__ __forceinline__ bool f_is_zero(double x);
+__device__ __forceinline__ bool f_is_zero(float x);
+
 // The reference's zero test on the centre Jacobian determinant of the force
 // phase (lulesh.cc:817-821). The fast variants test the determinant of 8
 // times the Jacobian in another summation order: zero for the same collapsed
@@ -151,7 +155,7 @@ __device__ __forceinline__ bool jacobian_singular(const R x[8], const R y[8], co
     const R det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) +
                   J[0][1] * (J[2][0] * J[1][2] - J[1][0] * J[2][2]) +
                   J[0][2] * (J[1][0] * J[2][1] - J[2][0] * J[1][1]);
-    return det == R(0);
+    return f_is_zero(det);
 #endif
 }
 
@@ -248,6 +252,8 @@ __device__ __forceinline__ double quot_refined(double a, double b) {
 #if LULESH_EXACT
 __device__ __forceinline__ bool f_lt(double x, double c) { return x < c; }
 __device__ __forceinline__ bool f_le(double x, double c) { return x <= c; }
+__device__ __forceinline__ bool f_neg(double x) { return x < 0.0; }
+__device__ __forceinline__ double nonneg_min(double a, double b) { return fmin(a, b); }
 __device__ __forceinline__ bool f_gt(double x, double c) { return x > c; }
 __device__ __forceinline__ bool f_ge(double x, double c) { return x >= c; }
 __device__ __forceinline__ bool f_abs_lt(double x, double c) { return fabs(x) < c; }
@@ -267,6 +273,12 @@ __device__ __forceinline__ bool f_gt(double x, double c) { return !f_le(x, c); }
 __device__ __forceinline__ bool f_ge(double x, double c) { return !f_lt(x, c); }
 __device__ __forceinline__ bool f_abs_lt(double x, double c) { return (dbits(x) & kMag) < dbits(c); }
 __device__ __forceinline__ bool f_is_zero(double x) { return (dbits(x) & kMag) == 0; }
+// x < 0 as IEEE (-0 is not negative)
+__device__ __forceinline__ bool f_neg(double x) { return dbits(x) < 0 && (dbits(x) & kMag) != 0; }
+// min of two non-negative, non-NaN doubles: their bit patterns order alike
+__device__ __forceinline__ double nonneg_min(double a, double b) {
+    return __longlong_as_double(min(dbits(a), dbits(b)));
+}
 #endif
 // two variables (the limiter); floats compare on the float pipe
 __device__ __forceinline__ bool f_vlt(double a, double b) {
@@ -281,6 +293,7 @@ __device__ __forceinline__ bool f_vlt(double a, double b) {
 __device__ __forceinline__ bool f_vlt(float a, float b) { return a < b; }
 __device__ __forceinline__ bool f_lt(float x, float c) { return x < c; }
 __device__ __forceinline__ bool f_gt(float x, float c) { return x > c; }
+__device__ __forceinline__ bool f_is_zero(float x) { return x == 0.0f; }
 
 __device__ __forceinline__ double recip_sqrt(double b) { return rsqrt(b); }
 __device__ __forceinline__ float recip_sqrt(float b) { return rsqrtf(b); }
@@ -901,6 +914,7 @@ template <bool UNIT_RHO>
 __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, int rep) {
     const lulesh_params& P = m.prm;
     double e_new = 0., p_new = 0., q_new = 0., bvc = 0., pbvc = 0.;
+    const bool vmin_on = !f_is_zero(P.eosvmin), vmax_on = !f_is_zero(P.eosvmax);
     for (int r = 0; r < rep; ++r) {
         // Each evaluation re-reads its inputs from memory as the reference's
         // EvalEOSInit does (lulesh.cc:1720-1727), and vnewc is made opaque,
@@ -914,8 +928,8 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
         double comp = rcp(vnewc) - 1.;
         const double vchalf = vnewc - delvc * .5;
         double compHalf = rcp(vchalf) - 1.;
-        if (P.eosvmin != 0. && f_le(vnewc, P.eosvmin)) compHalf = comp;
-        if (P.eosvmax != 0.0 && f_ge(vnewc, P.eosvmax)) {
+        if (vmin_on && f_le(vnewc, P.eosvmin)) compHalf = comp;
+        if (vmax_on && f_ge(vnewc, P.eosvmax)) {
             p_old = 0.;
             comp = 0.;
             compHalf = 0.;
@@ -987,6 +1001,7 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
     const lulesh_params& P = m.prm;
     const double cls = 2.0 / 3.0;
     double e_new = 0., p_new = 0., q_new = 0., vf = vnewc;
+    const bool vmin_on = !f_is_zero(P.eosvmin), vmax_on = !f_is_zero(P.eosvmax);
     for (int r = 0; r < rep; ++r) {
         asm volatile("" ::: "memory");
         asm volatile("" : "+d"(vnewc));
@@ -997,11 +1012,11 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
         double bvcf = cls * rcp(vnewc), bvch = cls * rcp(vchalf);
         double vh = vchalf;
         vf = vnewc;
-        if (P.eosvmin != 0. && f_le(vnewc, P.eosvmin)) {
+        if (vmin_on && f_le(vnewc, P.eosvmin)) {
             bvch = bvcf;
             vh = vnewc;
         }
-        if (P.eosvmax != 0.0 && f_ge(vnewc, P.eosvmax)) {
+        if (vmax_on && f_ge(vnewc, P.eosvmax)) {
             p_old = 0.;
             bvcf = bvch = cls;
             vh = 1.0;
@@ -1054,8 +1069,8 @@ __device__ __forceinline__ void dt_constraints(const lulesh_params& P, double ss
     double dtf = ss * ss;
     if (f_lt(vdov, 0.0)) dtf += qqc2 * arealg * arealg * vdov * vdov;
     dtf = div_sqrt(arealg, dtf);  // arealg / sqrt(dtf)
-    dtc = fmin(dtc, dtf);
-    dth = fmin(dth, quot(P.dvovmax, fabs(vdov) + 1.e-20));
+    dtc = nonneg_min(dtc, dtf);
+    dth = nonneg_min(dth, quot(P.dvovmax, fabs(vdov) + 1.e-20));
 }
 
 // Block-wide min of (a, b); the result is valid in thread 0.
@@ -1160,11 +1175,11 @@ __device__ __forceinline__ void node_update(const Mesh& m, int n, double fx, dou
 __device__ __forceinline__ void update_volume(const Mesh& m, int i, double vold, double relv) {
     const lulesh_params& P = m.prm;
     double vc = vold;
-    if (P.eosvmin != 0.0 && vc < P.eosvmin) vc = P.eosvmin;
-    if (P.eosvmax != 0.0 && vc > P.eosvmax) vc = P.eosvmax;
-    if (vc < 0.0) raise_error(m.result, i, PHASE_KINEMATICS);
+    if (!f_is_zero(P.eosvmin) && f_lt(vc, P.eosvmin)) vc = P.eosvmin;
+    if (!f_is_zero(P.eosvmax) && f_gt(vc, P.eosvmax)) vc = P.eosvmax;
+    if (f_neg(vc)) raise_error(m.result, i, PHASE_KINEMATICS);
     double vn = relv;
-    if (fabs(vn - 1.0) < P.v_cut) vn = 1.0;
+    if (f_abs_lt(vn - 1.0, P.v_cut)) vn = 1.0;
     m.v[i] = vn;
 }
 
