@@ -375,7 +375,9 @@ int lulesh_probe_pipe_rates(double out[5]);
  * inputs (no counterpart in the reference; accuracy tests compare the results
  * with correctly rounded host values): fn 0 reciprocal, 1 reciprocal cube
  * root, 2 square root, 3 reciprocal square root (inputs positive and normal
- * for 1-3), 4 the hardware seed of the reciprocal. n <= 2^26. */
+ * for 1-3), 4 the hardware seed of the reciprocal; 5 the mixed variant's
+ * double-to-float rounding, 6 and 7 the high and low floats of its float-pair
+ * split (results returned as doubles). n <= 2^26. */
 int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n);
 
 /* Selects the CUDA device used by handles created afterwards on this thread. */

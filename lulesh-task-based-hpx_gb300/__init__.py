@@ -418,7 +418,8 @@ def pipe_rates() -> dict:
     return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma"), list(out)))
 
 
-MATH_FUNCTIONS = {"rcp": 0, "rcbrt": 1, "sqrt": 2, "rsqrt": 3, "rcp_seed": 4}
+MATH_FUNCTIONS = {"rcp": 0, "rcbrt": 1, "sqrt": 2, "rsqrt": 3, "rcp_seed": 4, "narrow": 5, "split_hi": 6,
+                  "split_lo": 7}
 
 
 def probe_math(fn: str, x):

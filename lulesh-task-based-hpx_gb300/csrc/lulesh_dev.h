@@ -134,6 +134,8 @@ int launch_material(const Mesh& m, cudaStream_t s);
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
 int launch_mirror(const Mesh& m, cudaStream_t s);
 int launch_mirror_range(const Mesh& m, int first, int end, cudaStream_t s);  // nodes [first, end)
+// the float conversions on n inputs (probe.cu's lulesh_probe_math)
+int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t s);
 }  // namespace mixed
 
 // Device-side TimeIncrement for the graph form (time_increment.cu).

@@ -35,31 +35,15 @@ __device__ __forceinline__ void rel8(const float2* __restrict__ p, const int nl[
 }
 
 // The float-pair mirror of v, (hi, lo) = (fl(v), fl(v - hi)) with fl the
-// round-to-nearest-even conversion, computed on the integer pipe
-// (conversions between float and double occupy the FP64 pipe): rounding
-// the double's bit pattern to 24 significant bits (add half a unit of the
-// 29 dropped bits, or just under half when the kept last bit is even, then
-// clear them; a carry moves into the exponent as rounding does) gives
-// fl(v) exactly, and v - hi is one exact double subtraction. Bit for bit the
-// conversions' result for |v| in [2^-74, float's largest]; zeros map to
-// zeros and other values take the conversion instructions.
-__device__ __forceinline__ unsigned long long round_to_float_bits(unsigned long long b) {
-    return (b + 0x0FFFFFFFull + ((b >> 29) & 1ull)) & ~((1ull << 29) - 1ull);
-}
-__device__ __forceinline__ float float_from_rounded(unsigned long long b) {
-    const unsigned e = unsigned(b >> 52) & 0x7ffu;
-    return __uint_as_float((unsigned(b >> 32) & 0x80000000u) | ((e - 896u) << 23) |
-                           (unsigned(b >> 29) & 0x7fffffu));
-}
-
-// The rare inputs (magnitudes outside the range above) take the conversion
-// instructions in functions of their own: inlined, the compiler evaluates
-// them for every input and selects, and conversions issue on the FP64 pipe.
+// round-to-nearest-even conversion, on the integer pipe (narrow's rounding of
+// the bit pattern; v - hi is one exact double subtraction). Bit for bit the
+// conversions' result for |v| in [2^-74, float's largest], where lo is zero
+// or a normal float; zeros map to zeros and other values take the conversion
+// instructions out of line.
 __device__ __noinline__ float2 split_convert(double v) {
     const float hi = __double2float_rn(v);
     return make_float2(hi, __double2float_rn(v - double(hi)));
 }
-__device__ __noinline__ double widen_convert(float f) { return double(f); }
 
 __device__ __forceinline__ float2 split(double v) {
     const unsigned long long b = __double_as_longlong(v);
@@ -69,17 +53,6 @@ __device__ __forceinline__ float2 split(double v) {
     const unsigned long long hb = round_to_float_bits(b);
     const unsigned long long lb = __double_as_longlong(v - __longlong_as_double(hb));
     return make_float2(float_from_rounded(hb), (lb << 1) == 0ull ? 0.0f : float_from_rounded(round_to_float_bits(lb)));
-}
-
-// float -> double, exact, on the integer pipe for zeros and normal floats.
-__device__ __forceinline__ double widen(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    if ((u << 1) == 0u) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(u) << 32));
-    if (e == 0u || e == 0xffu) return widen_convert(f);
-    return __longlong_as_double(static_cast<long long>(
-        (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
-        (static_cast<unsigned long long>(e + 896u) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));
 }
 
 __device__ __forceinline__ void mirror_node(const Mesh& m, int n) {
@@ -193,12 +166,12 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     rel8(m.pxp, nl, x);
     rel8(m.pyp, nl, y);
     rel8(m.pzp, nl, z);
-    m.arealg[i] = double(char_length(x, y, z, float(volume)));
+    m.arealg[i] = widen(char_length(x, y, z, narrow(volume)));
     rel8(m.vxp, nl, xv);
     rel8(m.vyp, nl, yv);
     rel8(m.vzp, nl, zv);
     float g[6];
-    m.vdov[i] = double(gradients_vdov(x, y, z, xv, yv, zv, float(LD(m.volo + i) * relv), float(0.5 * dt), g));
+    m.vdov[i] = widen(gradients_vdov(x, y, z, xv, yv, zv, narrow(LD(m.volo + i) * relv), narrow(0.5 * dt), g));
     m.gvxi[i] = g[0];
     m.gveta[i] = g[1];
     m.gvzeta[i] = g[2];
@@ -297,6 +270,24 @@ int launch_material(const Mesh& m, cudaStream_t s) {
 }
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s) {
     k_material<<<m.matGrid, kMatBlock, 0, s>>>(m, first, end, accumulate ? 1 : 0);
+    return 1;
+}
+
+// The integer-pipe conversions evaluated on given inputs, for tests against
+// the host's round-to-nearest-even float conversion. fn: 5 narrow, 6 and 7
+// the high and low float of split (each returned as the double it equals).
+__global__ void k_math_probe(int fn, const double* __restrict__ in, double* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = in[i];
+    float r;
+    if (fn == 5) r = narrow(x);
+    else if (fn == 6) r = split(x).x;
+    else r = split(x).y;
+    out[i] = double(r);
+}
+int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t s) {
+    k_math_probe<<<blocks_for(n, 256), 256, 0, s>>>(fn, in, out, n);
     return 1;
 }
 

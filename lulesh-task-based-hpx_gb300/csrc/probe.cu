@@ -87,7 +87,7 @@ extern "C" int lulesh_probe_pipe_rates(double out[5]) {
 }
 
 extern "C" int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n) {
-    if (!in || !out || fn < 0 || fn > 4 || n < 1 || n > (int64_t(1) << 26)) return LULESH_EINVAL;
+    if (!in || !out || fn < 0 || fn > 7 || n < 1 || n > (int64_t(1) << 26)) return LULESH_EINVAL;
     const size_t bytes = sizeof(double) * size_t(n);
     double *d_in = nullptr, *d_out = nullptr;
     if (cudaMalloc(&d_in, bytes) != cudaSuccess) return LULESH_ENOMEM;
@@ -98,7 +98,8 @@ extern "C" int lulesh_probe_math(int32_t fn, const double* in, double* out, int6
     int st = LULESH_OK;
     if (cudaMemcpy(d_in, in, bytes, cudaMemcpyHostToDevice) != cudaSuccess) st = LULESH_ECUDA;
     if (st == LULESH_OK) {
-        lulesh::fp64::launch_math_probe(fn, d_in, d_out, int(n), nullptr);
+        if (fn <= 4) lulesh::fp64::launch_math_probe(fn, d_in, d_out, int(n), nullptr);
+        else lulesh::mixed::launch_math_probe(fn, d_in, d_out, int(n), nullptr);
         if (cudaGetLastError() != cudaSuccess ||
             cudaMemcpy(out, d_out, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = LULESH_ECUDA;

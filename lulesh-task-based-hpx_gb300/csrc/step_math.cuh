@@ -295,6 +295,41 @@ __device__ __forceinline__ bool f_lt(float x, float c) { return x < c; }
 __device__ __forceinline__ bool f_gt(float x, float c) { return x > c; }
 __device__ __forceinline__ bool f_is_zero(float x) { return x == 0.0f; }
 
+// Conversions between double and float on the integer pipe (conversion
+// instructions occupy the FP64 pipe on GB300). narrow rounds a double to
+// float, round to nearest even: add half a unit of the 29 dropped bits (just
+// under half when the kept last bit is even), clear them, and a carry moves
+// into the exponent as rounding does; bit for bit the conversion's result
+// for magnitudes whose float is normal (overflow gives the infinity). widen
+// is exact for zeros and normal floats. Zeros keep their sign; other inputs
+// take the conversion instruction in a function of its own (inlined, the
+// compiler would evaluate it for every input and select).
+__device__ __forceinline__ unsigned long long round_to_float_bits(unsigned long long b) {
+    return (b + 0x0FFFFFFFull + ((b >> 29) & 1ull)) & ~((1ull << 29) - 1ull);
+}
+__device__ __forceinline__ float float_from_rounded(unsigned long long b) {
+    const unsigned e = unsigned(b >> 52) & 0x7ffu;
+    return __uint_as_float((unsigned(b >> 32) & 0x80000000u) | ((e - 896u) << 23) |
+                           (unsigned(b >> 29) & 0x7fffffu));
+}
+__device__ __noinline__ float narrow_convert(double v) { return __double2float_rn(v); }
+__device__ __noinline__ double widen_convert(float f) { return double(f); }
+__device__ __forceinline__ float narrow(double v) {
+    const unsigned long long b = __double_as_longlong(v);
+    const unsigned e = unsigned(b >> 52) & 0x7ffu;
+    if ((b << 1) == 0ull) return __uint_as_float(unsigned(b >> 32));  // +-0
+    if (e < 897u || e > 1150u) return narrow_convert(v);
+    return float_from_rounded(round_to_float_bits(b));
+}
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if ((u << 1) == 0u) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(u) << 32));
+    if (e == 0u || e == 0xffu) return widen_convert(f);
+    return __longlong_as_double(static_cast<long long>(
+        (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
+        (static_cast<unsigned long long>(e + 896u) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));
+}
 __device__ __forceinline__ double recip_sqrt(double b) { return rsqrt(b); }
 __device__ __forceinline__ float recip_sqrt(float b) { return rsqrtf(b); }
 

@@ -62,3 +62,38 @@ def test_reciprocal_seed_bound(lulesh):
 def test_probe_rejects_bad_arguments(lulesh):
     with pytest.raises(lulesh.LuleshError):
         lulesh.probe_math("rcp", np.empty(0))
+
+
+def _conversion_inputs() -> np.ndarray:
+    """Doubles across float's whole range and beyond it: subnormal floats,
+    overflow, ties between two floats, zeros of both signs."""
+    rng = np.random.default_rng(31)
+    x = np.ldexp(rng.uniform(1.0, 2.0, N), rng.integers(-160, 140, N))
+    x[N // 2:] *= -1.0
+    ties = np.ldexp(rng.integers(1 << 23, 1 << 24, 4096) * 2.0 + 1.0, rng.integers(-120, 100, 4096) - 24)
+    x[:4096] = ties  # exactly halfway between two floats: round to even
+    x[4096:4100] = [0.0, -0.0, np.finfo(np.float32).max, -np.finfo(np.float32).max]
+    return x
+
+
+def test_narrow_is_round_to_nearest_even(lulesh):
+    """The mixed variant's integer-pipe double-to-float rounding equals the
+    conversion bit for bit (signed zeros and infinities included)."""
+    x = _conversion_inputs()
+    got = lulesh.probe_math("narrow", x)
+    with np.errstate(over="ignore"):
+        want = x.astype(np.float32).astype(np.float64)
+    assert np.array_equal(np.signbit(got), np.signbit(want))
+    assert np.array_equal(got, want)
+
+
+def test_split_is_the_float_pair(lulesh):
+    """split(v) = (fl(v), fl(v - fl(v))) bit for bit, where the pair is finite."""
+    x = _conversion_inputs()
+    x = x[np.abs(x) <= np.finfo(np.float32).max]
+    hi = lulesh.probe_math("split_hi", x)
+    lo = lulesh.probe_math("split_lo", x)
+    want_hi = x.astype(np.float32).astype(np.float64)
+    want_lo = (x - want_hi).astype(np.float32).astype(np.float64)
+    assert np.array_equal(hi, want_hi)
+    assert np.array_equal(lo, want_lo)
