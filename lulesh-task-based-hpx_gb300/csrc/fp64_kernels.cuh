@@ -100,7 +100,17 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     gather8(m.x, nl, x);
     gather8(m.y, nl, y);
     gather8(m.z, nl, z);
-    if (jacobian_singular(x, y, z)) raise_error(m.result, i, PHASE_FORCES);
+    // 8 x the centre Jacobian and its cofactors; the zero test on its
+    // determinant (lulesh.cc:817-821) in another summation order: zero for
+    // the same collapsed elements, though a near-singular element may round
+    // differently
+    double J[3][3], c[3][3];
+    dirs(x, J[0]);
+    dirs(y, J[1]);
+    dirs(z, J[2]);
+    cofactors(J, c);
+    if (f_is_zero(J[0][0] * c[0][0] + J[1][0] * c[1][0] + J[2][0] * c[2][0]))
+        raise_error(m.result, i, PHASE_FORCES);
     const double determ = LD(m.volo + i) * LD(m.v + i);
     if (f_le(determ, 0.0)) {
         raise_error(m.result, i, PHASE_FORCES);
@@ -108,9 +118,24 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     }
     double hg[8][4];
     {
-        double dvdx[8], dvdy[8], dvdz[8];
-        volume_derivs(dvdx, dvdy, dvdz, x, y, z);
-        hourgam_all(hg, x, y, z, dvdx, dvdy, dvdz, rcp(determ));
+        // hourglass vectors from the volume gradient (192 x dV/dx_k) and the
+        // mode sums scaled by volinv / 192
+        double hx[4], hy[4], hz[4], gx[8], gy[8], gz[8];
+        hourmod4(x, hx);
+        hourmod4(y, hy);
+        hourmod4(z, hz);
+        volume_gradient(J, c, hx, hy, hz, gx, gy, gz);
+        const double sc = rcp(determ) * (1.0 / 192.0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            hx[k] *= sc;
+            hy[k] *= sc;
+            hz[k] *= sc;
+        }
+        hourgam_mode_h<0>(hg, hx[0], hy[0], hz[0], gx, gy, gz);
+        hourgam_mode_h<1>(hg, hx[1], hy[1], hz[1], gx, gy, gz);
+        hourgam_mode_h<2>(hg, hx[2], hy[2], hz[2], gx, gy, gz);
+        hourgam_mode_h<3>(hg, hx[3], hy[3], hz[3], gx, gy, gz);
     }
     double fa[6][3];
     face_vectors(x, y, z, (LD(m.p + i) + LD(m.q + i)) * kInvNormalScale, fa);

@@ -548,6 +548,68 @@ __device__ __forceinline__ void hourmod4(const R v[8], R h[4]) {
     h[3] = q - p;                      // (- + - + + - + -)
 }
 
+#if !LULESH_EXACT
+// 192 times the gradient of the element volume with respect to each corner
+// (fast variants). With the body-diagonal sums A_d = sum_k s_dk x_k (the
+// columns of J = dirs, s_dk = xi, eta, zeta of corner k) and the hourglass
+// mode sums H_m = sum_k t_mk x_k (hourmod4's modes eta zeta, zeta xi, xi eta),
+// the trilinear hexahedron's volume, its integral of det(dx/dxi) over the
+// reference cube, is
+//   64 V = det(A1, A2, A3) + (det(A1, H3, H2) + det(H3, A2, H1) + det(H2, H1, A3)) / 3,
+// the value of the reference's CalcElemVolume (lulesh.cc:592-665) in another
+// form. Its gradient at corner k is sum_d s_dk dV/dA_d + sum_m t_mk dV/dH_m:
+// six vectors of cross products (c holds cof(J), whose column d is
+// A_{d+1} x A_{d+2}) and a sign transform over the corners, in place of
+// VoluDer's six products per component and corner (lulesh.cc:468-523).
+template <class R>
+__device__ __forceinline__ void cross_acc(const R u[3], const R v[3], R w[3]) {  // w += u x v
+    w[0] = fma(u[1], v[2], fma(-u[2], v[1], w[0]));
+    w[1] = fma(u[2], v[0], fma(-u[0], v[2], w[1]));
+    w[2] = fma(u[0], v[1], fma(-u[1], v[0], w[2]));
+}
+template <class R>
+__device__ __forceinline__ void volume_gradient(const R J[3][3], const R c[3][3], const R hx[4],
+                                                const R hy[4], const R hz[4], R gx[8], R gy[8],
+                                                R gz[8]) {
+    const R A[3][3] = {{J[0][0], J[1][0], J[2][0]}, {J[0][1], J[1][1], J[2][1]}, {J[0][2], J[1][2], J[2][2]}};
+    const R H[3][3] = {{hx[0], hy[0], hz[0]}, {hx[1], hy[1], hz[1]}, {hx[2], hy[2], hz[2]}};
+    R g[6][3];  // dV/dA_1..3, dV/dH_1..3, times 192
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g[0][a] = R(3) * c[a][0];
+        g[1][a] = R(3) * c[a][1];
+        g[2][a] = R(3) * c[a][2];
+        g[3][a] = g[4][a] = g[5][a] = R(0);
+    }
+    cross_acc(H[2], H[1], g[0]);
+    cross_acc(H[0], H[2], g[1]);
+    cross_acc(H[1], H[0], g[2]);
+    cross_acc(H[2], A[1], g[3]);
+    cross_acc(A[2], H[1], g[3]);
+    cross_acc(A[0], H[2], g[4]);
+    cross_acc(H[0], A[2], g[4]);
+    cross_acc(H[1], A[0], g[5]);
+    cross_acc(A[1], H[0], g[5]);
+    R* out[3] = {gx, gy, gz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // f = xi g1 + eta g2 + zeta g3 + eta zeta g4 + zeta xi g5 + xi eta g6 at the corners
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {  // zeta = -1 (corners 0-3), +1 (corners 4-7)
+            const R bx = h ? g[0][a] + g[4][a] : g[0][a] - g[4][a];
+            const R by = h ? g[1][a] + g[3][a] : g[1][a] - g[3][a];
+            const R p = bx + by, q = bx - by;
+            const R sv = h ? g[5][a] + g[2][a] : g[5][a] - g[2][a];  // xi eta g6 + zeta g3, xi = eta
+            const R tv = h ? g[2][a] - g[5][a] : -g[2][a] - g[5][a];  // xi = -eta
+            out[a][4 * h + 0] = sv - p;  // (-1, -1)
+            out[a][4 * h + 1] = tv + q;  // ( 1, -1)
+            out[a][4 * h + 2] = sv + p;  // ( 1,  1)
+            out[a][4 * h + 3] = tv - q;  // (-1,  1)
+        }
+    }
+}
+#endif
+
 // Hourglass shape vectors of mode M (lulesh.cc:988-1023) from the mode sums
 // hx, hy, hz of the coordinates, already multiplied by volinv: three
 // multiply-adds per corner.
