@@ -104,10 +104,10 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     // determinant (lulesh.cc:817-821) in another summation order: zero for
     // the same collapsed elements, though a near-singular element may round
     // differently
-    double J[3][3], c[3][3];
-    dirs(x, J[0]);
-    dirs(y, J[1]);
-    dirs(z, J[2]);
+    double J[3][3], c[3][3], hx[4], hy[4], hz[4];
+    walsh7(x, J[0], hx);
+    walsh7(y, J[1], hy);
+    walsh7(z, J[2], hz);
     cofactors(J, c);
     if (f_is_zero(J[0][0] * c[0][0] + J[1][0] * c[1][0] + J[2][0] * c[2][0]))
         raise_error(m.result, i, PHASE_FORCES);
@@ -120,10 +120,7 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     {
         // hourglass vectors from the volume gradient (192 x dV/dx_k) and the
         // mode sums scaled by volinv / 192
-        double hx[4], hy[4], hz[4], gx[8], gy[8], gz[8];
-        hourmod4(x, hx);
-        hourmod4(y, hy);
-        hourmod4(z, hz);
+        double gx[8], gy[8], gz[8];
         volume_gradient(J, c, hx, hy, hz, gx, gy, gz);
         const double sc = rcp(determ) * (1.0 / 192.0);
 #pragma unroll

@@ -549,6 +549,29 @@ __device__ __forceinline__ void hourmod4(const R v[8], R h[4]) {
 }
 
 #if !LULESH_EXACT
+// dirs(v, d) and hourmod4(v, h) together as a three-stage Walsh-Hadamard
+// transform over the corners' (xi, eta, zeta) signs: 23 adds for the 7
+// non-constant coefficients instead of 11 + 18.
+template <class R>
+__device__ __forceinline__ void walsh7(const R v[8], R d[3], R h[4]) {
+    // xi pairs of the four (eta, zeta) edges: corners (0,1), (3,2), (4,5), (7,6)
+    const R p00 = v[1] + v[0], m00 = v[1] - v[0], p10 = v[2] + v[3], m10 = v[2] - v[3];
+    const R p01 = v[5] + v[4], m01 = v[5] - v[4], p11 = v[6] + v[7], m11 = v[6] - v[7];
+    // eta, per zeta layer
+    const R pp0 = p10 + p00, pm0 = p10 - p00, mp0 = m10 + m00, mm0 = m10 - m00;
+    const R pp1 = p11 + p01, pm1 = p11 - p01, mp1 = m11 + m01, mm1 = m11 - m01;
+    // zeta
+    d[0] = mp1 + mp0;  // xi
+    d[1] = pm1 + pm0;  // eta
+    d[2] = pp1 - pp0;  // zeta
+    h[0] = pm1 - pm0;  // eta zeta
+    h[1] = mp1 - mp0;  // zeta xi
+    h[2] = mm1 + mm0;  // xi eta
+    h[3] = mm1 - mm0;  // xi eta zeta
+}
+#endif
+
+#if !LULESH_EXACT
 // 192 times the gradient of the element volume with respect to each corner
 // (fast variants). With the body-diagonal sums A_d = sum_k s_dk x_k (the
 // columns of J = dirs, s_dk = xi, eta, zeta of corner k) and the hourglass
