@@ -20,6 +20,7 @@
 // compensated sum and then promoted to double for the node update.
 #define LULESH_VARIANT mixed
 #define LULESH_EXACT 0
+#define LULESH_FLOAT_Q 1
 #include "step_math.cuh"
 
 namespace lulesh {

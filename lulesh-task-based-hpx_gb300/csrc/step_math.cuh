@@ -1021,6 +1021,25 @@ __device__ __forceinline__ double ss_guard(double ssc) {
 #endif
 }
 
+// Square root of the q terms' sound-speed expression (ss_guard's guard and
+// value). The mixed variant forms the linear and quadratic q coefficients
+// (ql, qq) in float, so its q terms take a float square root of the double
+// expression (two conversions and a float reciprocal square root instead of
+// the double sequence); the sound speed saved for the dt constraints stays
+// double.
+#ifndef LULESH_FLOAT_Q
+#define LULESH_FLOAT_Q 0
+#endif
+__device__ __forceinline__ double q_sound(double ssc) {
+#if LULESH_FLOAT_Q
+    if (f_le(ssc, .1111111e-36)) return .3333333e-18;
+    const float f = float(ssc);
+    return double(f * rsqrtf(f));
+#else
+    return ss_guard(ssc);
+#endif
+}
+
 // rep evaluations of EvalEOSAllInOneTask (lulesh.cc:1692-1871) for element i,
 // each from the saved state, then the sound speed and the save of
 // CalcSoundSpeedForElemsAndSaveTask (lulesh.cc:1873-1904). Returns ss.
@@ -1148,7 +1167,7 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
         if (f_lt(e_new, P.emin)) e_new = P.emin;
         const double pHalf = pressure(bvch, e_new, vnewc, P);
         if (f_gt(delvc, 0.)) q_new = 0.;
-        else q_new = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vh * pHalf), P)) * ql_old + qq_old;
+        else q_new = q_sound(over_rho<UNIT_RHO>(cls * (e_new + vh * pHalf), P)) * ql_old + qq_old;
         const double pq_half = pHalf + q_new;
         e_new = e_new + 0.5 * delvc * (3.0 * pq_old - 4.0 * pq_half);
         if (f_abs_lt(e_new, P.e_cut)) e_new = 0.0;
@@ -1157,13 +1176,13 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
         // corrector
         double q_tilde;
         if (f_gt(delvc, 0.)) q_tilde = 0.;
-        else q_tilde = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
+        else q_tilde = q_sound(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
         e_new = e_new - (7.0 * pq_old - 8.0 * pq_half + (p_new + q_tilde)) * (delvc * (1.0 / 6.0));
         if (f_abs_lt(e_new, P.e_cut)) e_new = 0.;
         if (f_lt(e_new, P.emin)) e_new = P.emin;
         p_new = pressure(bvcf, e_new, vnewc, P);
         if (f_le(delvc, 0.)) {
-            q_new = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
+            q_new = q_sound(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
             if (f_abs_lt(q_new, P.q_cut)) q_new = 0.;
         }
     }
