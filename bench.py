@@ -70,16 +70,16 @@ BYTES_PER_UNIT = {
 # DRAM bytes (read + write) per unit measured by ncu at s=100, where every
 # array exceeds L2 (profiles/dram_traffic_s100.md); scaled by units per launch.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"forces": 272, "nodes": 342, "kinematics": 142, "material": 183},
-    "mixed": {"forces": 188, "nodes": 275, "kinematics": 156, "material": 149},
+    "fp64": {"forces": 271, "nodes": 343, "kinematics": 141, "material": 183},
+    "mixed": {"forces": 188, "nodes": 275, "kinematics": 157, "material": 149},
 }
 # FP64-pipe instructions per unit (thread level: sm__inst_executed_pipe_fp64
 # x 32 / units) measured by ncu at s=100 for the branch-free kernels; the
 # material kernel's count depends on the state (EOS repeats, compressing
 # elements), so it has none here.
 FP64_INSTR_PER_UNIT = {
-    "fp64": {"forces": 725.0, "nodes": 35.7, "kinematics": 336.0},
-    "mixed": {"forces": 8.0, "nodes": 38.9, "kinematics": 96.0},
+    "fp64": {"forces": 671.0, "nodes": 35.7, "kinematics": 332.0},
+    "mixed": {"forces": 8.0, "nodes": 27.0, "kinematics": 90.0},
 }
 # Double-precision operations per unit of the reference's formulation (adds,
 # multiplies, divides, square and cube roots each counted once), from
