@@ -24,6 +24,11 @@ struct Launchers {
     int (*material)(const Mesh&, cudaStream_t);
     int (*forces_range)(const Mesh&, int, int, cudaStream_t);
     int (*material_range)(const Mesh&, int, int, bool, cudaStream_t);
+    // the resident loop's geometry form (fast double variant; else null):
+    // kinematics store the element geometry the next forces read
+    int (*forces_geo)(const Mesh&, cudaStream_t);
+    int (*kinematics_geo)(const Mesh&, double, cudaStream_t);
+    int (*geometry)(const Mesh&, cudaStream_t);
 };
 
 Launchers launchers_for(int precision) {
@@ -31,15 +36,19 @@ Launchers launchers_for(int precision) {
         case LULESH_FP64:
             return {lulesh::fp64::launch_forces, lulesh::fp64::launch_nodes,
                     lulesh::fp64::launch_kinematics, lulesh::fp64::launch_material,
-                    lulesh::fp64::launch_forces_range, lulesh::fp64::launch_material_range};
+                    lulesh::fp64::launch_forces_range, lulesh::fp64::launch_material_range,
+                    lulesh::fp64::launch_forces_geo, lulesh::fp64::launch_kinematics_geo,
+                    lulesh::fp64::launch_geometry};
         case LULESH_FP64_EXACT:
             return {lulesh::fp64x::launch_forces, lulesh::fp64x::launch_nodes,
                     lulesh::fp64x::launch_kinematics, lulesh::fp64x::launch_material,
-                    lulesh::fp64x::launch_forces_range, lulesh::fp64x::launch_material_range};
+                    lulesh::fp64x::launch_forces_range, lulesh::fp64x::launch_material_range,
+                    nullptr, nullptr, nullptr};
         default:
             return {lulesh::mixed::launch_forces, lulesh::mixed::launch_nodes,
                     lulesh::mixed::launch_kinematics, lulesh::mixed::launch_material,
-                    lulesh::mixed::launch_forces_range, lulesh::mixed::launch_material_range};
+                    lulesh::mixed::launch_forces_range, lulesh::mixed::launch_material_range,
+                    nullptr, nullptr, nullptr};
     }
 }
 
@@ -81,6 +90,10 @@ struct lulesh_dev {
     cudaStream_t mstream = nullptr;            // downloads of the material phase's outputs
     int32_t* matOrderSlab = nullptr;           // [N_e] slab-major material order (arena)
     Launchers L{};
+    // m.geo holds the geometry of the current coordinates (set by the
+    // geometry form's kinematics and the geometry pass; cleared by anything
+    // that writes coordinates or runs the phases another way)
+    bool geo_valid = false;
     // device-side timing (lulesh_dev_profile_begin/end)
     bool profiling = false;
     cudaEvent_t ev[5] = {};
@@ -157,6 +170,7 @@ int check_view(const lulesh_domain_view* v) {
 // only measures.
 void carve_mesh(Mesh& m, Arena& a, int precision, int ne, int nn) {
     const bool mixed = precision == LULESH_MIXED;
+    m.geo = nullptr;  // a single handle's layout adds it
     for (double** f : {&m.x, &m.y, &m.z, &m.xd, &m.yd, &m.zd, &m.xdd, &m.ydd, &m.zdd, &m.fx, &m.fy,
                        &m.fz})
         *f = a.take<double>(nn);
@@ -199,6 +213,7 @@ void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     // slab launch of lulesh_leapfrog with one thread per element
     m.partials = a.take<lulesh::DtPartial>(std::max(matGrid, lulesh::blocks_for(ne, lulesh::kMatBlock)));
     m.result = a.take<StepResult>(1);
+    m.geo = d->L.forces_geo ? a.take<double>(size_t(lulesh::kGeoWords) * ne) : nullptr;
     d->d_time = a.take<DevTime>(1);
     d->d_verify = a.take<double>(4);
     d->matOrderSlab = a.take<int32_t>(ne);
@@ -318,12 +333,19 @@ int run_cycle(lulesh_dev* d, double dt) {
     const Mesh& m = d->m;
     const bool prof = d->profiling;
     CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
+    const bool geo = d->L.forces_geo != nullptr;
     if (prof) CK(cudaEventRecord(d->ev[0], d->stream));
-    d->launches += d->L.forces(m, d->stream);
+    if (geo) {
+        if (!d->geo_valid) d->launches += d->L.geometry(m, d->stream);
+        d->launches += d->L.forces_geo(m, d->stream);
+    } else {
+        d->launches += d->L.forces(m, d->stream);
+    }
     if (prof) CK(cudaEventRecord(d->ev[1], d->stream));
     d->launches += d->L.nodes(m, dt, d->stream);
     if (prof) CK(cudaEventRecord(d->ev[2], d->stream));
-    d->launches += d->L.kinematics(m, dt, d->stream);
+    d->launches += geo ? d->L.kinematics_geo(m, dt, d->stream) : d->L.kinematics(m, dt, d->stream);
+    d->geo_valid = geo;
     if (prof) CK(cudaEventRecord(d->ev[3], d->stream));
     d->launches += d->L.material(m, d->stream);
     if (prof) CK(cudaEventRecord(d->ev[4], d->stream));
@@ -352,10 +374,11 @@ int build_graph(lulesh_dev* d) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
     int k = 0;
+    const bool geo = d->L.forces_geo != nullptr;
     k += lulesh::launch_time_increment(d->d_time, gm.result, d->stream);
-    k += d->L.forces(gm, d->stream);
+    k += geo ? d->L.forces_geo(gm, d->stream) : d->L.forces(gm, d->stream);
     k += d->L.nodes(gm, 0.0, d->stream);
-    k += d->L.kinematics(gm, 0.0, d->stream);
+    k += geo ? d->L.kinematics_geo(gm, 0.0, d->stream) : d->L.kinematics(gm, 0.0, d->stream);
     k += d->L.material(gm, d->stream);
     k += lulesh::launch_time_finish(d->d_time, gm.result, d->stream);
     cudaError_t ce = cudaStreamEndCapture(d->stream, &g);
@@ -509,6 +532,7 @@ int lulesh_dev_verify(lulesh_dev* d, int32_t cycle, lulesh_verify_result* out) {
 int lulesh_dev_upload(lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask) {
     if (!d || !v || v->numElem != d->m.numElem || v->numNode != d->m.numNode) return LULESH_EINVAL;
     if (mask & LULESH_F_MESH) return LULESH_EINVAL;  // the mesh is fixed at creation
+    d->geo_valid = false;
     for (const Copy& c : groups(d->m, v, mask)) {
         if (!c.host) return LULESH_EINVAL;
         CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, d->stream));
@@ -544,6 +568,7 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     if (!d || !v || !v->time || v->numElem != d->m.numElem || v->numNode != d->m.numNode)
         return LULESH_EINVAL;
     if (!(v->time->deltatime > 0.0)) return LULESH_EINVAL;
+    d->geo_valid = false;  // the coordinates come from the host buffers
     const auto in = groups(d->m, v, LULESH_F_STEP_IN);
     const auto out_nodes = groups(d->m, v, LULESH_F_POS | LULESH_F_VEL | LULESH_F_ACC | LULESH_F_FORCE);
     const auto out_kin = groups(d->m, v, LULESH_F_V | LULESH_F_KIN);
@@ -692,6 +717,13 @@ int lulesh_dev_run_graph(lulesh_dev* d, lulesh_time_state* ts, int32_t max_cycle
     const int32_t start = ts->cycle;
     CK(cudaMemsetAsync(d->m.result, 0, sizeof(StepResult), d->stream));
     CK(cudaMemcpyAsync(d->d_time, d->h_time, sizeof(DevTime), cudaMemcpyHostToDevice, d->stream));
+    if (d->L.forces_geo) {
+        if (!d->geo_valid) {
+            d->launches += d->L.geometry(d->m, d->stream);
+            CK(cudaGetLastError());
+        }
+        d->geo_valid = true;
+    }
     for (;;) {
         for (int k = 0; k < sync_every; ++k) {
             CK(cudaGraphLaunch(d->graph, d->stream));
@@ -718,6 +750,7 @@ int lulesh_dev_run_graph(lulesh_dev* d, lulesh_time_state* ts, int32_t max_cycle
 int lulesh_dev_phase(lulesh_dev* d, int32_t phase, double dt) {
     if (!d) return LULESH_EINVAL;
     const Mesh& m = d->m;
+    d->geo_valid = false;  // the single phases use the forming kernels
     CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
     switch (phase) {
         case LULESH_PHASE_FORCES: d->launches += d->L.forces(m, d->stream); break;

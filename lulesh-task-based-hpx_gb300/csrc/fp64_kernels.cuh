@@ -86,30 +86,88 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     }
 }
 #else
-// Fast variant: stress plus hourglass corner force of element i summed in
-// registers and stored once (corner-major fsx, fsy, fsz). The stress force
-// (p + q) n enters through the six face vectors scaled by (p + q) / 8, each
-// corner's stress is the start of its hourglass multiply-add chain.
-// Elements that fail the determinant test store nothing: the step reports
-// the error and its state is not used.
-__device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
+// Element geometry (fast variant): everything the force phase derives from
+// the corner coordinates alone. J holds the body-diagonal sums (8 x the
+// centre Jacobian, columns along xi, eta, zeta) and h the hourglass mode sums
+// of each coordinate, both from one Walsh-Hadamard transform; c the cofactors
+// of J; fa the six faces' t x s, unscaled. The kinematics phase forms the
+// same geometry of the updated coordinates for its own needs (J and c for
+// the Q gradients and vdov, fa for the characteristic length) and, in the
+// resident loop, stores it for the next cycle's force phase, whose
+// coordinates those are. Every path forms it with the same operations, so
+// stored and recomputed geometry are the same bits.
+struct ElemGeo {
+    double J[3][3], c[3][3], h[3][4], fa[6][3];
+};
+
+__device__ __forceinline__ void elem_geometry(const double x[8], const double y[8], const double z[8],
+                                              ElemGeo& g) {
+    walsh7(x, g.J[0], g.h[0]);
+    walsh7(y, g.J[1], g.h[1]);
+    walsh7(z, g.J[2], g.h[2]);
+    cofactors(g.J, g.c);
+    face_txs<0, 1, 2, 3>(x, y, z, g.fa[0]);
+    face_txs<0, 4, 5, 1>(x, y, z, g.fa[1]);
+    face_txs<1, 5, 6, 2>(x, y, z, g.fa[2]);
+    face_txs<2, 6, 7, 3>(x, y, z, g.fa[3]);
+    face_txs<3, 7, 4, 0>(x, y, z, g.fa[4]);
+    face_txs<4, 7, 6, 5>(x, y, z, g.fa[5]);
+}
+
+// Mesh::geo word q of element i is geo[q * numElem + i]: J, c, h, fa in
+// row-major order.
+__device__ __forceinline__ void geo_store(const Mesh& m, int i, const ElemGeo& g) {
     const size_t N = (size_t)m.numElem;
-    int nl[8];
-    load_nodelist(m.nodelist, i, nl);
-    double x[8], y[8], z[8];
-    gather8(m.x, nl, x);
-    gather8(m.y, nl, y);
-    gather8(m.z, nl, z);
-    // 8 x the centre Jacobian and its cofactors; the zero test on its
-    // determinant (lulesh.cc:817-821) in another summation order: zero for
-    // the same collapsed elements, though a near-singular element may round
-    // differently
-    double J[3][3], c[3][3], hx[4], hy[4], hz[4];
-    walsh7(x, J[0], hx);
-    walsh7(y, J[1], hy);
-    walsh7(z, J[2], hz);
-    cofactors(J, c);
-    if (f_is_zero(J[0][0] * c[0][0] + J[1][0] * c[1][0] + J[2][0] * c[2][0]))
+    double* o = m.geo + i;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            o[(3 * a + d) * N] = g.J[a][d];
+            o[(9 + 3 * a + d) * N] = g.c[a][d];
+        }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) o[(18 + 4 * a + k) * N] = g.h[a][k];
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) o[(30 + 3 * f + d) * N] = g.fa[f][d];
+}
+__device__ __forceinline__ void geo_load(const Mesh& m, int i, ElemGeo& g) {
+    const size_t N = (size_t)m.numElem;
+    const double* o = m.geo + i;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            g.J[a][d] = LD(o + (3 * a + d) * N);
+            g.c[a][d] = LD(o + (9 + 3 * a + d) * N);
+        }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) g.h[a][k] = LD(o + (18 + 4 * a + k) * N);
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g.fa[f][d] = LD(o + (30 + 3 * f + d) * N);
+}
+
+// Stress plus hourglass corner force of element i from its geometry, summed
+// in registers and stored once (corner-major fsx, fsy, fsz). The zero test
+// on the centre Jacobian's determinant (lulesh.cc:817-821) is taken in
+// another summation order: zero for the same collapsed elements, though a
+// near-singular element may round differently. The hourglass vectors come
+// from the volume gradient (192 x dV/dx_k) and the mode sums scaled by
+// volinv / 192. The stress force (p + q) n enters through the face vectors
+// scaled by (p + q) / 8 and starts each corner's hourglass multiply-add
+// chain. Elements that fail a test store nothing: the step reports the
+// error and its state is not used.
+__device__ __forceinline__ void forces_from_geo(const Mesh& m, int i, const int nl[8], const ElemGeo& g) {
+    const size_t N = (size_t)m.numElem;
+    if (f_is_zero(g.J[0][0] * g.c[0][0] + g.J[1][0] * g.c[1][0] + g.J[2][0] * g.c[2][0]))
         raise_error(m.result, i, PHASE_FORCES);
     const double determ = LD(m.volo + i) * LD(m.v + i);
     if (f_le(determ, 0.0)) {
@@ -118,16 +176,14 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
     }
     double hg[8][4];
     {
-        // hourglass vectors from the volume gradient (192 x dV/dx_k) and the
-        // mode sums scaled by volinv / 192
-        double gx[8], gy[8], gz[8];
-        volume_gradient(J, c, hx, hy, hz, gx, gy, gz);
+        double gx[8], gy[8], gz[8], hx[4], hy[4], hz[4];
+        volume_gradient(g.J, g.c, g.h[0], g.h[1], g.h[2], gx, gy, gz);
         const double sc = rcp(determ) * (1.0 / 192.0);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            hx[k] *= sc;
-            hy[k] *= sc;
-            hz[k] *= sc;
+            hx[k] = g.h[0][k] * sc;
+            hy[k] = g.h[1][k] * sc;
+            hz[k] = g.h[2][k] * sc;
         }
         hourgam_mode_h<0>(hg, hx[0], hy[0], hz[0], gx, gy, gz);
         hourgam_mode_h<1>(hg, hx[1], hy[1], hz[1], gx, gy, gz);
@@ -135,7 +191,11 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
         hourgam_mode_h<3>(hg, hx[3], hy[3], hz[3], gx, gy, gz);
     }
     double fa[6][3];
-    face_vectors(x, y, z, (LD(m.p + i) + LD(m.q + i)) * kInvNormalScale, fa);
+    const double scale = (LD(m.p + i) + LD(m.q + i)) * kInvNormalScale;
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) fa[f][d] = g.fa[f][d] * scale;
     const double coefficient = -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) * rcbrt_pos(determ);
     double* outs[3] = {m.fsx, m.fsy, m.fsz};
     const double* vels[3] = {m.xd, m.yd, m.zd};
@@ -148,6 +208,43 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) outs[a][k * N + i] = f[k];
     }
+}
+
+// Forces of element i from its coordinates (geometry formed here).
+__device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    ElemGeo g;
+    {
+        double x[8], y[8], z[8];
+        gather8(m.x, nl, x);
+        gather8(m.y, nl, y);
+        gather8(m.z, nl, z);
+        elem_geometry(x, y, z, g);
+    }
+    forces_from_geo(m, i, nl, g);
+}
+
+// Forces of element i from the stored geometry.
+__device__ __forceinline__ void forces_geo_elem(const Mesh& m, int i) {
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    ElemGeo g;
+    geo_load(m, i, g);
+    forces_from_geo(m, i, nl, g);
+}
+
+// Stores the geometry of element i's current coordinates.
+__device__ __forceinline__ void geometry_elem(const Mesh& m, int i) {
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    double x[8], y[8], z[8];
+    gather8(m.x, nl, x);
+    gather8(m.y, nl, y);
+    gather8(m.z, nl, z);
+    ElemGeo g;
+    elem_geometry(x, y, z, g);
+    geo_store(m, i, g);
 }
 #endif
 
@@ -179,6 +276,7 @@ __device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt) {
 // CalcKinematicsForElemsTask (lulesh.cc:1169-1275) and
 // CalcMonotonicQGradientsForElemsTask (lulesh.cc:1277-1418) of element i:
 // both read the same updated node positions and velocities.
+#if LULESH_EXACT
 __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt) {
     int nl[8];
     load_nodelist(m.nodelist, i, nl);
@@ -206,6 +304,56 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
     m.dxzeta[i] = g[5];
     update_volume(m, i, vold, relv);
 }
+#else
+// Characteristic length 4 V / sqrt(largest face measure) from the faces'
+// t x s: the reference's face measure is 4 |t x s|^2 (Lagrange's identity),
+// so the length is 2 V / sqrt(max |t x s|^2).
+__device__ __forceinline__ double char_length_faces(const double fa[6][3], double volume) {
+    double cl = fa[0][0] * fa[0][0] + fa[0][1] * fa[0][1] + fa[0][2] * fa[0][2];
+#pragma unroll
+    for (int f = 1; f < 6; ++f)
+        cl = nonneg_max(cl, fa[f][0] * fa[f][0] + fa[f][1] * fa[f][1] + fa[f][2] * fa[f][2]);
+    return div_sqrt(2.0 * volume, cl);
+}
+
+// Kinematics of element i; STORE_GEO: also store the element geometry of the
+// updated coordinates for the next force phase (Mesh::geo).
+template <bool STORE_GEO>
+__device__ __forceinline__ void kinematics_fast(const Mesh& m, int i, double dt) {
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    double relv, vold;
+    ElemGeo g;
+    {
+        double x[8], y[8], z[8];
+        gather8(m.x, nl, x);
+        gather8(m.y, nl, y);
+        gather8(m.z, nl, z);
+        const double volume = hex_volume(x, y, z);
+        relv = quot_refined(volume, LD(m.volo + i));
+        vold = m.v[i];
+        m.vnew[i] = relv;
+        m.delv[i] = relv - vold;
+        elem_geometry(x, y, z, g);
+        m.arealg[i] = char_length_faces(g.fa, volume);
+    }
+    if (STORE_GEO) geo_store(m, i, g);
+    double xv[8], yv[8], zv[8];
+    gather8(m.xd, nl, xv);
+    gather8(m.yd, nl, yv);
+    gather8(m.zd, nl, zv);
+    double gr[6];
+    m.vdov[i] = gradients_vdov_xc(g.J, g.c, xv, yv, zv, LD(m.volo + i) * relv, 0.5 * dt, gr);
+    m.dvxi[i] = gr[0];
+    m.dveta[i] = gr[1];
+    m.dvzeta[i] = gr[2];
+    m.dxxi[i] = gr[3];
+    m.dxeta[i] = gr[4];
+    m.dxzeta[i] = gr[5];
+    update_volume(m, i, vold, relv);
+}
+__device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt) { kinematics_fast<false>(m, i, dt); }
+#endif
 
 // Material phase of the element at position t of the repeat-count order
 // (matOrder): Q limiter and q terms, rep EOS passes, sound speed and save;
@@ -252,6 +400,28 @@ __global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
     if (i < m.numElem) kinematics_elem(m, i, dt);
 }
 
+#if !LULESH_EXACT
+// The resident loop's form: forces from the stored geometry, kinematics that
+// store it, and the pass that forms it from the current coordinates.
+__global__ void __launch_bounds__(kForceBlock) k_forces_geo(Mesh m) {
+    if (m.dtime && !m.dtime->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.numElem) forces_geo_elem(m, i);
+}
+__global__ void __launch_bounds__(kKinBlock) k_kinematics_geo(Mesh m, double dt) {
+    if (m.dtime) {
+        if (!m.dtime->active) return;
+        dt = m.dtime->deltatime;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.numElem) kinematics_fast<true>(m, i, dt);
+}
+__global__ void __launch_bounds__(kForceBlock) k_geometry(Mesh m) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m.numElem) geometry_elem(m, i);
+}
+#endif
+
 // Elements visited in repeat-count order so a warp's lanes run the same
 // number of EOS passes; the dt minima end in a last-block reduction.
 __global__ void __launch_bounds__(kMatBlock) k_material(Mesh m, int first, int end, int accumulate) {
@@ -287,6 +457,20 @@ int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cu
     k_material<<<m.matGrid, kMatBlock, 0, s>>>(m, first, end, accumulate ? 1 : 0);
     return 1;
 }
+#if !LULESH_EXACT
+int launch_forces_geo(const Mesh& m, cudaStream_t s) {
+    k_forces_geo<<<blocks_for(m.numElem, kForceBlock), kForceBlock, 0, s>>>(m);
+    return 1;
+}
+int launch_kinematics_geo(const Mesh& m, double dt, cudaStream_t s) {
+    k_kinematics_geo<<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt);
+    return 1;
+}
+int launch_geometry(const Mesh& m, cudaStream_t s) {
+    k_geometry<<<blocks_for(m.numElem, kForceBlock), kForceBlock, 0, s>>>(m);
+    return 1;
+}
+#endif
 
 }  // namespace LULESH_VARIANT
 }  // namespace lulesh

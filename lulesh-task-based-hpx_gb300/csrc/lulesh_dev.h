@@ -81,6 +81,9 @@ struct Mesh {
     // scratch, double path
     double *fsx, *fsy, *fsz, *fhx, *fhy, *fhz;
     double *dvxi, *dveta, *dvzeta, *dxxi, *dxeta, *dxzeta;
+    // fast double path of a single handle: the element geometry of the
+    // current coordinates, kGeoWords arrays of numElem doubles (else null)
+    double* geo;
     // mixed path: float-pair mirrors (hi, lo) of positions and velocities
     float2 *pxp, *pyp, *pzp, *vxp, *vyp, *vzp;
     // scratch, mixed path
@@ -93,6 +96,10 @@ struct Mesh {
     int32_t matGrid; // blocks of the material kernel (= entries of partials)
     lulesh_params prm;
 };
+
+// Words of element geometry stored per element (Mesh::geo): direction sums
+// (9), their cofactors (9), hourglass mode sums (12), face vectors (18).
+constexpr int kGeoWords = 48;
 
 // Launch configuration shared by host and device code.
 constexpr int kForceBlock = 128;
@@ -114,6 +121,12 @@ int launch_material(const Mesh& m, cudaStream_t s);
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
 // the fast helpers on n inputs (probe.cu's lulesh_probe_math)
 int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t s);
+// the resident loop's form: kinematics that also stores the element geometry
+// of the updated coordinates (m.geo), forces that read it, and the pass that
+// forms it from the current coordinates when it is stale
+int launch_forces_geo(const Mesh& m, cudaStream_t s);
+int launch_kinematics_geo(const Mesh& m, double dt, cudaStream_t s);
+int launch_geometry(const Mesh& m, cudaStream_t s);
 }  // namespace fp64
 namespace fp64x {
 int launch_forces(const Mesh& m, cudaStream_t s);

@@ -875,6 +875,45 @@ __device__ __forceinline__ R vel_grad_trace(const R xh[8], const R yh[8], const 
     return dxx + dyy + dzz;
 }
 
+#if !LULESH_EXACT
+// gradients_vdov from the coordinates' direction sums X and their cofactors
+// c = cof(X), computed by the caller (fast variants).
+template <class R>
+__device__ __forceinline__ R gradients_vdov_xc(const R X[3][3], const R cx[3][3], const R xv[8],
+                                               const R yv[8], const R zv[8], R vol, R dt2, R g[6]) {
+    R V[3][3], c[3][3];
+    dirs(xv, V[0]);
+    dirs(yv, V[1]);
+    dirs(zv, V[2]);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) c[a][d] = cx[a][d];
+    const R pt = R(256.0) * R(1.e-36);
+    const R vol16 = R(16.0) * vol;
+    const R n64 = rcp(vol + R(1.e-36)) * R(0.015625);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        g[3 + d] = vol16 * recip_sqrt(c[0][d] * c[0][d] + c[1][d] * c[1][d] + c[2][d] * c[2][d] + pt);
+        g[d] = (c[0][d] * V[0][d] + c[1][d] * V[1][d] + c[2][d] * V[2][d]) * n64;
+    }
+    R J[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) J[a][d] = X[a][d] - dt2 * V[a][d];
+    cofactors(J, c);
+    const R det = J[0][0] * c[0][0] + J[0][1] * c[0][1] + J[0][2] * c[0][2];
+    R num = c[0][0] * V[0][0];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (a + d > 0) num = num + c[a][d] * V[a][d];
+    return quot(num, det);
+}
+#endif
+
 // Q gradients g (as q_gradients) and vdov, the trace of the velocity
 // gradient at the half-step geometry x - dt2 v (lulesh.cc:1221-1232), of one
 // element. Exact variant: the reference's two computations. Fast variants,
@@ -899,38 +938,16 @@ __device__ __forceinline__ R gradients_vdov(const R x[8], const R y[8], const R 
     }
     return vel_grad_trace(xh, yh, zh, xv, yv, zv);
 #else
-    R X[3][3], V[3][3], c[3][3];
+    R X[3][3], c[3][3];
     dirs(x, X[0]);
     dirs(y, X[1]);
     dirs(z, X[2]);
-    dirs(xv, V[0]);
-    dirs(yv, V[1]);
-    dirs(zv, V[2]);
     cofactors(X, c);
-    const R pt = R(256.0) * R(1.e-36);
-    const R vol16 = R(16.0) * vol;
-    const R n64 = rcp(vol + R(1.e-36)) * R(0.015625);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        g[3 + d] = vol16 * recip_sqrt(c[0][d] * c[0][d] + c[1][d] * c[1][d] + c[2][d] * c[2][d] + pt);
-        g[d] = (c[0][d] * V[0][d] + c[1][d] * V[1][d] + c[2][d] * V[2][d]) * n64;
-    }
-    R J[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) J[a][d] = X[a][d] - dt2 * V[a][d];
-    cofactors(J, c);
-    const R det = J[0][0] * c[0][0] + J[0][1] * c[0][1] + J[0][2] * c[0][2];
-    R num = c[0][0] * V[0][0];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-            if (a + d > 0) num = num + c[a][d] * V[a][d];
-    return quot(num, det);
+    return gradients_vdov_xc(X, c, xv, yv, zv, vol, dt2, g);
 #endif
 }
+
+
 
 // --- material ------------------------------------------------------------
 
