@@ -62,15 +62,17 @@ UNIT = "zone-cycles/s"
 
 # Algorithmic HBM bytes per unit (element, or node for the node kernel) of each
 # kernel: every array touched once per launch, node fields counted once per
-# node (N_n / N_e ~ 1), neighbour re-reads assumed to hit L2.
+# node (N_n / N_e ~ 1), neighbour re-reads assumed to hit L2. The double
+# path's resident loop passes 48 doubles of element geometry per element from
+# kinematics (written) to the next force phase (read instead of the positions).
 BYTES_PER_UNIT = {
-    "fp64": {"forces": 320, "nodes": 381, "kinematics": 184, "material": 204},
+    "fp64": {"forces": 680, "nodes": 381, "kinematics": 568, "material": 204},
     "mixed": {"forces": 224, "nodes": 333, "kinematics": 184, "material": 180},
 }
 # DRAM bytes (read + write) per unit measured by ncu at s=100, where every
 # array exceeds L2 (profiles/dram_traffic_s100.md); scaled by units per launch.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"forces": 271, "nodes": 343, "kinematics": 141, "material": 183},
+    "fp64": {"forces": 648, "nodes": 342, "kinematics": 506, "material": 183},
     "mixed": {"forces": 188, "nodes": 275, "kinematics": 157, "material": 149},
 }
 # FP64-pipe instructions per unit (thread level: sm__inst_executed_pipe_fp64
@@ -78,7 +80,7 @@ TRAFFIC_PER_UNIT = {
 # material kernel's count depends on the state (EOS repeats, compressing
 # elements), so it has none here.
 FP64_INSTR_PER_UNIT = {
-    "fp64": {"forces": 671.0, "nodes": 35.7, "kinematics": 332.0},
+    "fp64": {"forces": 512.0, "nodes": 35.7, "kinematics": 368.0},
     "mixed": {"forces": 8.0, "nodes": 27.0, "kinematics": 90.0},
 }
 # Double-precision operations per unit of the reference's formulation (adds,
