@@ -94,6 +94,8 @@ struct lulesh_dev {
     // geometry form's kinematics and the geometry pass; cleared by anything
     // that writes coordinates or runs the phases another way)
     bool geo_valid = false;
+    // lulesh_leapfrog's copies of the uploaded coordinates (with m.geo)
+    double* stage[3] = {nullptr, nullptr, nullptr};
     // device-side timing (lulesh_dev_profile_begin/end)
     bool profiling = false;
     cudaEvent_t ev[5] = {};
@@ -214,6 +216,7 @@ void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     m.partials = a.take<lulesh::DtPartial>(std::max(matGrid, lulesh::blocks_for(ne, lulesh::kMatBlock)));
     m.result = a.take<StepResult>(1);
     m.geo = d->L.forces_geo ? a.take<double>(size_t(lulesh::kGeoWords) * ne) : nullptr;
+    for (double*& p : d->stage) p = d->L.forces_geo ? a.take<double>(nn) : nullptr;
     d->d_time = a.take<DevTime>(1);
     d->d_verify = a.take<double>(4);
     d->matOrderSlab = a.take<int32_t>(ne);
@@ -568,7 +571,12 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     if (!d || !v || !v->time || v->numElem != d->m.numElem || v->numNode != d->m.numNode)
         return LULESH_EINVAL;
     if (!(v->time->deltatime > 0.0)) return LULESH_EINVAL;
-    d->geo_valid = false;  // the coordinates come from the host buffers
+    // The coordinates come from the host buffers. With the geometry form they
+    // upload into copies, and elements whose corners the host left as the
+    // previous step made them reuse the geometry that step stored.
+    const bool geo = d->L.forces_geo != nullptr;
+    const bool have_geo = geo && d->geo_valid;
+    d->geo_valid = false;
     const auto in = groups(d->m, v, LULESH_F_STEP_IN);
     const auto out_nodes = groups(d->m, v, LULESH_F_POS | LULESH_F_VEL | LULESH_F_ACC | LULESH_F_FORCE);
     const auto out_kin = groups(d->m, v, LULESH_F_V | LULESH_F_KIN);
@@ -628,22 +636,38 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
             }
             const bool node = c.bytes == sizeof(double) * size_t(m.numNode);
             const int64_t a = node ? node_done : e0, b = node ? n1 : e1;
+            double* dst = static_cast<double*>(c.dev);
+            if (geo) {
+                if (dst == m.x) dst = d->stage[0];
+                else if (dst == m.y) dst = d->stage[1];
+                else if (dst == m.z) dst = d->stage[2];
+            }
             if (b > a)
-                CK(cudaMemcpyAsync(static_cast<double*>(c.dev) + a, static_cast<const double*>(c.host) + a,
-                                   sizeof(double) * size_t(b - a), cudaMemcpyHostToDevice, d->cstream));
+                CK(cudaMemcpyAsync(dst + a, static_cast<const double*>(c.host) + a, sizeof(double) * size_t(b - a),
+                                   cudaMemcpyHostToDevice, d->cstream));
         }
         CK(cudaEventRecord(d->ev_slab[sl], d->cstream));
         CK(cudaStreamWaitEvent(d->stream, d->ev_slab[sl], 0));
         if (d->precision == LULESH_MIXED)
             d->launches += lulesh::mixed::launch_mirror_range(m, int(node_done), int(n1), d->stream);
-        d->launches += d->L.forces_range(m, int(e0), int(e1), d->stream);
+        if (geo)
+            d->launches += lulesh::fp64::launch_forces_stage_range(m, d->stage[0], d->stage[1], d->stage[2], int(e0),
+                                                                   int(e1), have_geo, d->stream);
+        else
+            d->launches += d->L.forces_range(m, int(e0), int(e1), d->stream);
         node_done = n1;
+    }
+    if (geo) {  // the uploaded coordinates become the device's (after every slab compared them)
+        double* cur[3] = {m.x, m.y, m.z};
+        for (int k = 0; k < 3; ++k)
+            CK(cudaMemcpyAsync(cur[k], d->stage[k], sizeof(double) * size_t(m.numNode), cudaMemcpyDeviceToDevice,
+                               d->stream));
     }
     if (e_in) CK(cudaMemcpyAsync(e_in->dev, e_in->host, e_in->bytes, cudaMemcpyHostToDevice, d->cstream));
     CK(cudaEventRecord(d->ev_e, d->cstream));
     d->launches += d->L.nodes(m, dt, d->stream);
     CK(cudaEventRecord(d->ev_nodes, d->stream));
-    d->launches += d->L.kinematics(m, dt, d->stream);
+    d->launches += geo ? d->L.kinematics_geo(m, dt, d->stream) : d->L.kinematics(m, dt, d->stream);
     CK(cudaEventRecord(d->ev_kin, d->stream));
     CK(cudaStreamWaitEvent(d->cstream, d->ev_nodes, 0));
     for (const Copy& c : out_nodes)
@@ -678,6 +702,7 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     }
     v->time->dtcourant = d->h_result->dtcourant;
     v->time->dthydro = d->h_result->dthydro;
+    d->geo_valid = geo;
     return LULESH_OK;
 }
 

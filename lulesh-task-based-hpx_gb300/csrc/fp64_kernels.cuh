@@ -234,6 +234,34 @@ __device__ __forceinline__ void forces_geo_elem(const Mesh& m, int i) {
     forces_from_geo(m, i, nl, g);
 }
 
+// Forces of element i in lulesh_leapfrog: the coordinates just uploaded from
+// the host (sx, sy, sz) are the step's; where they equal, bit for bit, the
+// device's own coordinates at all 8 corners (the previous step's results, the
+// host having left them unchanged) and the stored geometry is that of the
+// device's coordinates (have_geo), the stored geometry is used, else it is
+// formed from the uploaded coordinates.
+__device__ __forceinline__ void forces_stage_elem(const Mesh& m, const double* __restrict__ sx,
+                                                  const double* __restrict__ sy,
+                                                  const double* __restrict__ sz, int i, bool have_geo) {
+    int nl[8];
+    load_nodelist(m.nodelist, i, nl);
+    double x[8], y[8], z[8];
+    gather8(sx, nl, x);
+    gather8(sy, nl, y);
+    gather8(sz, nl, z);
+    bool same = have_geo;
+    if (same) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            same = same && dbits(x[k]) == dbits(LD(m.x + nl[k])) && dbits(y[k]) == dbits(LD(m.y + nl[k])) &&
+                   dbits(z[k]) == dbits(LD(m.z + nl[k]));
+    }
+    ElemGeo g;
+    if (same) geo_load(m, i, g);
+    else elem_geometry(x, y, z, g);
+    forces_from_geo(m, i, nl, g);
+}
+
 // Stores the geometry of element i's current coordinates.
 __device__ __forceinline__ void geometry_elem(const Mesh& m, int i) {
     int nl[8];
@@ -416,6 +444,12 @@ __global__ void __launch_bounds__(kKinBlock) k_kinematics_geo(Mesh m, double dt)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m.numElem) kinematics_fast<true>(m, i, dt);
 }
+__global__ void __launch_bounds__(kForceBlock) k_forces_stage(Mesh m, const double* sx, const double* sy,
+                                                               const double* sz, int first, int end,
+                                                               int have_geo) {
+    const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < end) forces_stage_elem(m, sx, sy, sz, i, have_geo != 0);
+}
 __global__ void __launch_bounds__(kForceBlock) k_geometry(Mesh m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m.numElem) geometry_elem(m, i);
@@ -464,6 +498,13 @@ int launch_forces_geo(const Mesh& m, cudaStream_t s) {
 }
 int launch_kinematics_geo(const Mesh& m, double dt, cudaStream_t s) {
     k_kinematics_geo<<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt);
+    return 1;
+}
+int launch_forces_stage_range(const Mesh& m, const double* sx, const double* sy, const double* sz, int first,
+                              int end, bool have_geo, cudaStream_t s) {
+    if (end <= first) return 0;
+    k_forces_stage<<<blocks_for(end - first, kForceBlock), kForceBlock, 0, s>>>(m, sx, sy, sz, first, end,
+                                                                                have_geo ? 1 : 0);
     return 1;
 }
 int launch_geometry(const Mesh& m, cudaStream_t s) {

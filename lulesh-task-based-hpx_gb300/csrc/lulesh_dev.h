@@ -127,6 +127,11 @@ int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t
 int launch_forces_geo(const Mesh& m, cudaStream_t s);
 int launch_kinematics_geo(const Mesh& m, double dt, cudaStream_t s);
 int launch_geometry(const Mesh& m, cudaStream_t s);
+// lulesh_leapfrog's force phase over elements [first, end): coordinates from
+// the uploaded copies sx, sy, sz, stored geometry where they match m.x, m.y,
+// m.z and have_geo
+int launch_forces_stage_range(const Mesh& m, const double* sx, const double* sy, const double* sz, int first,
+                              int end, bool have_geo, cudaStream_t s);
 }  // namespace fp64
 namespace fp64x {
 int launch_forces(const Mesh& m, cudaStream_t s);

@@ -235,6 +235,34 @@ def test_leapfrog_on_host_buffers_equals_resident_run(lulesh, precision):
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
 
 
+def test_leapfrog_with_host_changed_coordinates(lulesh):
+    """lulesh_leapfrog reuses the element geometry its previous step stored
+    only for elements whose 8 corners the host left as that step made them.
+    With one node moved on the host between two calls, the drop-in run stays
+    bit for bit the device-resident run given the same move by upload."""
+    a, b = lulesh.HostDomain(10), lulesh.HostDomain(10)
+    dev_a, dev_b = lulesh.Device(a, "fp64"), lulesh.Device(b, "fp64")
+    node = 137  # an interior node (plane 1, row 1, column 5 of s=10)
+    for cycle in range(12):
+        if cycle == 6:
+            dev_b.download(lulesh.F_POS)
+            for dom in (a, b):
+                dom.x[node] += 1e-7
+                dom.z[node] -= 2e-7
+            dev_b.upload(lulesh.F_POS)
+        a.time_increment()
+        dev_a.leapfrog()
+        dev_b.run(b.time_state.cycle + 1)
+    dev_b.download()
+    assert a.cycle == b.cycle == 12
+    for f in ("time", "deltatime", "dtcourant", "dthydro"):
+        assert getattr(a.time_state, f) == getattr(b.time_state, f), f
+    for f in NODE + ELEM:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    dev_a.close()
+    dev_b.close()
+
+
 @pytest.mark.parametrize("s", [16, 30])
 def test_mixed_full_run(lulesh, golden_results, s):
     g = _golden(golden_results, s)
