@@ -191,6 +191,10 @@ int finish_admit(lulesh_batch* b, int slot, size_t off, size_t bytes, Mesh m, co
         b->pool.release(off, bytes);
         return code;
     };
+    if (m.geo) {  // the fast double variant's element geometry, before the first force phase
+        b->launches += lulesh::fp64::launch_geometry(m, b->stream);
+        if (cudaGetLastError() != cudaSuccess) return release(LULESH_ECUDA);
+    }
     if (cudaMemcpyAsync(b->d_meshes + slot, b->h_meshes + slot, sizeof(Mesh), cudaMemcpyHostToDevice, b->stream) !=
             cudaSuccess ||
         cudaMemcpyAsync(b->d_times + slot, b->h_times + slot, sizeof(DevTime), cudaMemcpyHostToDevice, b->stream) !=

@@ -83,9 +83,16 @@ __global__ void __launch_bounds__(kBatchMaxBlock, 1) kb_phase(BatchCtl c, int gr
                 }
             } else {
                 for (int k = threadIdx.x; k < tile.count; k += blockDim.x) {
+#if LULESH_GEO_FORM
+                    // the fast double variant's geometry form (each instance's
+                    // geometry formed at admission, kept by its kinematics)
+                    if (PHASE == 0) forces_geo_elem(m, tile.first + k);
+                    if (PHASE == 2) kinematics_fast<true>(m, tile.first + k, s_dt);
+#else
                     if (PHASE == 0) forces_elem(m, tile.first + k);
-                    if (PHASE == 1) nodes_node(m, tile.first + k, s_dt);
                     if (PHASE == 2) kinematics_elem(m, tile.first + k, s_dt);
+#endif
+                    if (PHASE == 1) nodes_node(m, tile.first + k, s_dt);
                 }
             }
         }

@@ -172,7 +172,7 @@ int check_view(const lulesh_domain_view* v) {
 // only measures.
 void carve_mesh(Mesh& m, Arena& a, int precision, int ne, int nn) {
     const bool mixed = precision == LULESH_MIXED;
-    m.geo = nullptr;  // a single handle's layout adds it
+    m.geo = nullptr;
     for (double** f : {&m.x, &m.y, &m.z, &m.xd, &m.yd, &m.zd, &m.xdd, &m.ydd, &m.zdd, &m.fx, &m.fy,
                        &m.fz})
         *f = a.take<double>(nn);
@@ -203,6 +203,8 @@ void carve_mesh(Mesh& m, Arena& a, int precision, int ne, int nn) {
             for (double** f : {&m.fhx, &m.fhy, &m.fhz}) *f = a.take<double>(8 * size_t(ne));
         for (double** f : {&m.dvxi, &m.dveta, &m.dvzeta, &m.dxxi, &m.dxeta, &m.dxzeta})
             *f = a.take<double>(ne);
+        // the fast double variant's element geometry (kinematics -> next forces)
+        if (precision == LULESH_FP64) m.geo = a.take<double>(size_t(lulesh::kGeoWords) * ne);
     }
 }
 
@@ -215,7 +217,6 @@ void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     // slab launch of lulesh_leapfrog with one thread per element
     m.partials = a.take<lulesh::DtPartial>(std::max(matGrid, lulesh::blocks_for(ne, lulesh::kMatBlock)));
     m.result = a.take<StepResult>(1);
-    m.geo = d->L.forces_geo ? a.take<double>(size_t(lulesh::kGeoWords) * ne) : nullptr;
     for (double*& p : d->stage) p = d->L.forces_geo ? a.take<double>(nn) : nullptr;
     d->d_time = a.take<DevTime>(1);
     d->d_verify = a.take<double>(4);

@@ -99,6 +99,7 @@ __device__ __forceinline__ void forces_elem(const Mesh& m, int i) {
 struct ElemGeo {
     double J[3][3], c[3][3], h[3][4], fa[6][3];
 };
+#define LULESH_GEO_FORM 1
 
 __device__ __forceinline__ void elem_geometry(const double x[8], const double y[8], const double z[8],
                                               ElemGeo& g) {

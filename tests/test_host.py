@@ -162,7 +162,10 @@ def test_batch_footprint_and_loud_failure_without_gpu(lulesh):
     f = [lulesh.Batch.footprint(p, s) for p in ("fp64", "mixed") for s in (16, 64, 150)]
     assert f[0] < f[1] < f[2] and f[3] < f[4] < f[5]
     assert f[5] < f[2]  # float temporaries take less memory
-    assert f[2] / 150 ** 3 < 800  # bytes per element of the double path
+    # bytes per element of the double path: about 560 of state and scratch,
+    # plus 384 of element geometry kept from kinematics to the next forces
+    assert f[2] / 150 ** 3 < 1000
+    assert f[5] / 150 ** 3 < 600  # the mixed path keeps no geometry
     with pytest.raises(lulesh.LuleshError) as ei:
         lulesh.Batch.footprint("fp64", 0)
     assert ei.value.status == lulesh.EINVAL
