@@ -263,6 +263,34 @@ def test_leapfrog_with_host_changed_coordinates(lulesh):
     dev_b.close()
 
 
+def test_geometry_hand_offs_between_entry_points(lulesh):
+    """The element geometry the double path keeps between phases stays valid
+    across the entry points that keep the coordinates (drop-in call, host
+    loop, graph loop) and is formed again after one that writes them (an
+    upload): a run that moves between them equals the plain host-loop run bit
+    for bit."""
+    a, b = lulesh.HostDomain(10), lulesh.HostDomain(10)
+    dev_a, dev_b = lulesh.Device(a, "fp64"), lulesh.Device(b, "fp64")
+    for _ in range(3):
+        a.time_increment()
+        dev_a.leapfrog()
+    dev_a.run(a.time_state.cycle + 3)
+    dev_a.run_graph(a.time_state.cycle + 3, 2)
+    dev_a.download()
+    dev_a.upload()
+    dev_a.run(a.time_state.cycle + 3)
+    dev_a.download()
+    dev_b.run(12)
+    dev_b.download()
+    assert a.cycle == b.cycle == 12
+    for f in ("time", "deltatime", "dtcourant", "dthydro"):
+        assert getattr(a.time_state, f) == getattr(b.time_state, f), f
+    for f in NODE + ELEM:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    dev_a.close()
+    dev_b.close()
+
+
 @pytest.mark.parametrize("s", [16, 30])
 def test_mixed_full_run(lulesh, golden_results, s):
     g = _golden(golden_results, s)
