@@ -410,24 +410,8 @@ __device__ __forceinline__ void face_txs(const R x[8], const R y[8], const R z[8
 constexpr double kInvNormalScale = LULESH_EXACT ? 0.0625 : 0.125;
 
 #if !LULESH_EXACT
-// The six faces' t x s (face_txs) times scale, faces in the reference's
-// order 0123, 0451, 1562, 2673, 3740, 4765.
-template <class R>
-__device__ __forceinline__ void face_vectors(const R x[8], const R y[8], const R z[8], R scale,
-                                             R fa[6][3]) {
-    face_txs<0, 1, 2, 3>(x, y, z, fa[0]);
-    face_txs<0, 4, 5, 1>(x, y, z, fa[1]);
-    face_txs<1, 5, 6, 2>(x, y, z, fa[2]);
-    face_txs<2, 6, 7, 3>(x, y, z, fa[3]);
-    face_txs<3, 7, 4, 0>(x, y, z, fa[4]);
-    face_txs<4, 7, 6, 5>(x, y, z, fa[5]);
-#pragma unroll
-    for (int f = 0; f < 6; ++f)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) fa[f][c] *= scale;
-}
-
-// Component c of the corner sums of face_vectors: each corner adds its
+// Component c of the corner sums of the six faces' t x s (faces in the
+// reference's order 0123, 0451, 1562, 2673, 3740, 4765): each corner adds its
 // three faces, and the four face pairs that two corners share are added
 // once (corners 0,1 share faces 0123 and 0451, corners 2,3 faces 0123 and
 // 2673, corners 4,5 faces 0451 and 4765, corners 6,7 faces 2673 and 4765).
