@@ -412,10 +412,13 @@ int new_handle(int32_t precision, int ne, int nn, lulesh_dev** out) {
     if (!d) return LULESH_ENOMEM;
     d->precision = precision;
     d->L = launchers_for(precision);
-    // 8 material blocks per SM: with the elements in repeat-count order this
-    // balanced the grid-stride loop best in a sweep of 5 to 28 per SM, for
-    // both the double and the mixed kernel (1.6 waves for the latter)
-    const int matGrid = std::max(1, std::min(lulesh::blocks_for(ne, lulesh::kMatBlock), sms * 8));
+    // Material blocks per SM of the grid-stride launch (elements in
+    // repeat-count order; 6 blocks of 78 registers fit per SM): a sweep of
+    // 6, 8, 12 per SM and one thread per element at s=150 gave the double
+    // kernel 1.38, 1.34, 1.37, 1.51 ms and the mixed kernel 0.92, 0.98, 0.95,
+    // 1.08 ms
+    const int mat_per_sm = precision == LULESH_MIXED ? 6 : 8;
+    const int matGrid = std::max(1, std::min(lulesh::blocks_for(ne, lulesh::kMatBlock), sms * mat_per_sm));
     Arena measure;
     layout(d, measure, ne, nn, matGrid);
     d->arena_bytes = measure.used;
