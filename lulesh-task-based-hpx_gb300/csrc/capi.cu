@@ -539,7 +539,7 @@ int lulesh_dev_verify(lulesh_dev* d, int32_t cycle, lulesh_verify_result* out) {
 int lulesh_dev_upload(lulesh_dev* d, const lulesh_domain_view* v, uint32_t mask) {
     if (!d || !v || v->numElem != d->m.numElem || v->numNode != d->m.numNode) return LULESH_EINVAL;
     if (mask & LULESH_F_MESH) return LULESH_EINVAL;  // the mesh is fixed at creation
-    d->geo_valid = false;
+    if (mask & LULESH_F_POS) d->geo_valid = false;  // the element geometry follows the coordinates
     for (const Copy& c : groups(d->m, v, mask)) {
         if (!c.host) return LULESH_EINVAL;
         CK(cudaMemcpyAsync(c.dev, c.host, c.bytes, cudaMemcpyHostToDevice, d->stream));

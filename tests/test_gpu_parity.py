@@ -266,9 +266,9 @@ def test_leapfrog_with_host_changed_coordinates(lulesh):
 def test_geometry_hand_offs_between_entry_points(lulesh):
     """The element geometry the double path keeps between phases stays valid
     across the entry points that keep the coordinates (drop-in call, host
-    loop, graph loop) and is formed again after one that writes them (an
-    upload): a run that moves between them equals the plain host-loop run bit
-    for bit."""
+    loop, graph loop, an upload of other fields) and is formed again after
+    one that writes them (an upload of the coordinates): a run that moves
+    between them equals the plain host-loop run bit for bit."""
     a, b = lulesh.HostDomain(10), lulesh.HostDomain(10)
     dev_a, dev_b = lulesh.Device(a, "fp64"), lulesh.Device(b, "fp64")
     for _ in range(3):
@@ -277,8 +277,11 @@ def test_geometry_hand_offs_between_entry_points(lulesh):
     dev_a.run(a.time_state.cycle + 3)
     dev_a.run_graph(a.time_state.cycle + 3, 2)
     dev_a.download()
+    dev_a.upload(lulesh.F_EPQ)  # coordinates untouched: the geometry stays
+    dev_a.run(a.time_state.cycle + 1)
+    dev_a.download()
     dev_a.upload()
-    dev_a.run(a.time_state.cycle + 3)
+    dev_a.run(a.time_state.cycle + 2)
     dev_a.download()
     dev_b.run(12)
     dev_b.download()
