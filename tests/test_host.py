@@ -173,3 +173,17 @@ def test_batch_footprint_and_loud_failure_without_gpu(lulesh):
         with pytest.raises(lulesh.LuleshError) as ei:
             lulesh.Batch("fp64", 1 << 20, 4)
         assert ei.value.status == lulesh.ENODEV
+
+
+def test_largest_problem_size(lulesh):
+    """Indices are int32 as in the reference (Index_t): the 8 s^3 corner
+    entries fit up to s = 645, and the library takes s <= 640, refusing
+    larger cubes before any allocation. At s = 640 the double path's problem
+    takes 248 GB, within a GB300's 280 GB."""
+    assert 8 * 645 ** 3 < 2 ** 31 <= 8 * 646 ** 3
+    f = lulesh.Batch.footprint("fp64", 640)
+    assert 240e9 < f < 260e9
+    for call in (lambda: lulesh.Batch.footprint("fp64", 641), lambda: lulesh.HostDomain(641)):
+        with pytest.raises(lulesh.LuleshError) as ei:
+            call()
+        assert ei.value.status == lulesh.EINVAL
