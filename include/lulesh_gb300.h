@@ -157,7 +157,11 @@ typedef struct lulesh_verify_result {
 /* Allocates device mirrors of the Domain arrays the step touches and uploads
  * all of them (constant topology and the full mutable state). Replaces the
  * reference's per-cycle malloc/free of temporaries (lulesh.cc:2017-2022,
- * lulesh.h:203-214): scratch is allocated once here. */
+ * lulesh.h:203-214): scratch is allocated once here. A LULESH_FP64 handle
+ * also keeps each element's geometry between the kinematics and the next
+ * force phase (48 doubles per element) and copies of the node coordinates
+ * for lulesh_leapfrog: lulesh_batch_footprint(LULESH_FP64, s) plus
+ * 24 (s + 1)^3 bytes in all. */
 int lulesh_dev_create(const lulesh_domain_view* host, int32_t precision, lulesh_dev** out);
 void lulesh_dev_destroy(lulesh_dev* dev);
 
@@ -191,7 +195,10 @@ int lulesh_dev_step(lulesh_dev* dev, double deltatime, double* dtcourant, double
  * view->time->deltatime, downloads every field the step writes and stores
  * dtcourant/dthydro into view->time. The copies overlap the cycle: the
  * upload runs on two streams, node fields stream back while the element
- * phases run and the kinematic fields while the material phase runs. On
+ * phases run and the kinematic fields while the material phase runs. With
+ * LULESH_FP64, elements whose 8 corner coordinates equal those the previous
+ * call left on the device reuse the element geometry it stored; the others
+ * form it from the uploaded coordinates (same results either way). On
  * LULESH_EVOLUME (where the reference exits) the host fields hold the
  * partly advanced state and view->time's dt constraints are unchanged. */
 int lulesh_leapfrog(lulesh_dev* dev, lulesh_domain_view* host);
@@ -240,10 +247,13 @@ typedef struct lulesh_batch_tuning {
  * problems at once. */
 int lulesh_batch_create(int32_t precision, uint64_t pool_bytes, int32_t max_slots, lulesh_batch** out);
 void lulesh_batch_destroy(lulesh_batch* b);
-/* Device bytes one s^3 problem takes in a pool of this precision. */
+/* Device bytes one s^3 problem takes in a pool of this precision (for
+ * LULESH_FP64 including its element geometry, 384 bytes per element). */
 int lulesh_batch_footprint(int32_t precision, int32_t s, uint64_t* bytes);
-/* Builds the problem (Domain::Domain on the host), copies it into the pool
- * and makes it active. LULESH_ENOMEM when the pool or the slots are full. */
+/* Builds the problem on the device in its pool block (the state
+ * Domain::Domain makes, bit for bit; the region runs of the reference's
+ * rand() sequence are drawn on the host) and makes it active. LULESH_ENOMEM
+ * when the pool or the slots are full. */
 int lulesh_batch_admit(lulesh_batch* b, const lulesh_problem* p, int32_t* slot);
 /* Admits an existing host Domain (a view as for lulesh_dev_create, with
  * view->time set): its whole state is copied into the pool. stoptime > 0 and
