@@ -60,17 +60,29 @@ sys.path.insert(0, str(ROOT / "oracle"))
 METRIC = "FOM zone-cycles/s at s=150 (FP64 vs mixed) + batched-ensemble zone-cycles/s"
 UNIT = "zone-cycles/s"
 
-# Algorithmic HBM bytes per unit (element, or node for the node kernel) of each
-# kernel: every array touched once per launch, node fields counted once per
-# node (N_n / N_e ~ 1), neighbour re-reads assumed to hit L2. The double
-# path's resident loop passes 48 doubles of element geometry per element from
-# kinematics (written) to the next force phase (read instead of the positions).
+# Algorithmic HBM bytes per unit (element, or node for the node kernel) of the
+# four-kernel step: the compulsory traffic of the step's own arrays, each
+# touched once per launch, node fields once per node (N_n / N_e ~ 1),
+# neighbour re-reads as L2 hits. Double: force 320 (node list 32, node
+# positions and velocities 48, p q v volo ss elemMass 48, 24 corner forces
+# 192), nodes 332, kinematics + Q gradients 184, material 184: 1,020 bytes per
+# zone-cycle. Mixed: float corner forces (-96 in forces and nodes) and float
+# Q gradients (-24 in kinematics and material): 780.
 BYTES_PER_UNIT = {
+    "fp64": {"forces": 320, "nodes": 332, "kinematics": 184, "material": 184},
+    "mixed": {"forces": 224, "nodes": 236, "kinematics": 160, "material": 160},
+}
+STEP_BYTES_PER_ZONE_CYCLE = {"fp64": 1020, "mixed": 780}
+# What this implementation's layout moves on top of that: the double path's
+# resident loop passes 48 doubles of element geometry per element from
+# kinematics (written) to the next force phase (read instead of the node
+# positions), and the mixed path reads float-pair node mirrors.
+LAYOUT_BYTES_PER_UNIT = {
     "fp64": {"forces": 680, "nodes": 381, "kinematics": 568, "material": 204},
     "mixed": {"forces": 224, "nodes": 333, "kinematics": 184, "material": 180},
 }
 # DRAM bytes (read + write) per unit measured by ncu at s=100, where every
-# array exceeds L2 (profiles/dram_traffic_s100.md); scaled by units per launch.
+# array exceeds L2; scaled by units per launch.
 TRAFFIC_PER_UNIT = {
     "fp64": {"forces": 648, "nodes": 342, "kinematics": 506, "material": 183},
     "mixed": {"forces": 188, "nodes": 275, "kinematics": 157, "material": 149},
@@ -214,16 +226,29 @@ def mean_rep(lul, dom) -> float:
     return float(rep.mean())
 
 
+def sig4(x: float) -> float:
+    """x rounded to 4 significant digits."""
+    return float(f"{x:.4g}")
+
+
 def roofline(prof: dict, precision: str, ne: int, nn: int, rep_avg: float,
-             fp64_peak: float = FP64_PEAK_TFLOPS, fp64_kind: str = "earlier probe") -> dict:
+             fp64_peak: float = FP64_PEAK_TFLOPS, fp64_kind: str = "earlier probe",
+             ms_per_step: float | None = None) -> dict:
     km = prof["kernel_ms"]
     cyc = max(prof["cycles"], 1)
     dom = max(km, key=km.get)
     units = nn if dom == "nodes" else ne
     avg_s = km[dom] / cyc / 1e3
     bytes_launch = BYTES_PER_UNIT[precision][dom] * units
+    layout_launch = LAYOUT_BYTES_PER_UNIT[precision][dom] * units
     peak, kind = hbm_peak()
     achieved = bytes_launch / avg_s / 1e9
+    step = None
+    if ms_per_step:
+        step_gbs = STEP_BYTES_PER_ZONE_CYCLE[precision] * ne / (ms_per_step / 1e3) / 1e9
+        step = {"achieved": round(step_gbs, 1), "frac": sig4(step_gbs / peak),
+                "bytes_per_zone_cycle": STEP_BYTES_PER_ZONE_CYCLE[precision],
+                "note": "the whole cycle: algorithmic bytes per zone-cycle x elements / ms_per_step"}
     if dom == "material":
         flops = FLOPS_PER_UNIT["material_base"] + FLOPS_PER_UNIT["material_per_rep"] * rep_avg
     else:
@@ -241,11 +266,15 @@ def roofline(prof: dict, precision: str, ne: int, nn: int, rep_avg: float,
                              f"DFMA issue rate, {fp64_kind} (lulesh_probe_pipe_rates)"}
     return {
         "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
-        "unit": "GB/s", "frac": round(achieved / peak, 4),
+        "unit": "GB/s", "frac": sig4(achieved / peak),
         "traffic": tpu * units if tpu else None,
         "traffic_note": "ncu dram bytes per unit at s=100 x units per launch" if tpu else None,
         "peak_kind": f"{kind} ({'MEASURED_PEAKS.json hbm_gbs' if kind == 'measured' else 'recipe fallback'})",
-        "bytes_per_launch": bytes_launch, "avg_launch_ms": round(km[dom] / cyc, 4),
+        "bytes_per_launch": bytes_launch, "bytes_per_unit": BYTES_PER_UNIT[precision][dom],
+        "avg_launch_ms": round(km[dom] / cyc, 4),
+        "frac_layout": sig4(layout_launch / avg_s / 1e9 / peak),
+        "layout_bytes_per_unit": LAYOUT_BYTES_PER_UNIT[precision][dom],
+        "step": step,
         "kernel_share": {k: round(v / max(sum(km.values()), 1e-30), 4) for k, v in km.items()},
         "reference_flops_tflops": round(tflops, 4),
         "fp64_pipe": fp64_pipe,
@@ -267,6 +296,11 @@ def time_device(lul, dom, dev, steps: int, world: int, graph: bool = False) -> d
         raise RuntimeError(f"ran {n} of {steps} cycles (stoptime reached?)")
     prof["max_ms"] = max_over_ranks(prof["total_ms"], world)
     return prof
+
+
+def workload(s: int, r: int) -> str:
+    """The workload name both arms print (config.workload)."""
+    return f"Sedov blast --s {s} --r {r} (b=1, c=1), one LagrangeLeapFrog cycle per step"
 
 
 def fom(value: float) -> dict:
@@ -351,7 +385,8 @@ def run_ours(args) -> None:
                  "ms_per_step": round(mprof["max_ms"] / K, 4),
                  "speedup_vs_fp64": round(mvalue / value, 3), "fom": fom(mvalue),
                  "kernel_ms_per_step": {k: round(v / K, 4) for k, v in mprof["kernel_ms"].items()},
-                 "roofline": roofline(mprof, "mixed", ne, nn, rep_avg, fp64_peak, "measured live")}
+                 "roofline": roofline(mprof, "mixed", ne, nn, rep_avg, fp64_peak, "measured live",
+                                      ms_per_step=mprof["max_ms"] / K)}
         mdev.close()
         mdom.close()
 
@@ -367,6 +402,9 @@ def run_ours(args) -> None:
                 res["vs_single_problem"] = round(res["value"] / single, 3)
             res["value_all_ranks"] = round(res["value"] * world, 1)
             batched[prec] = res
+        # the mixed ensemble against the double ensemble of the same seed
+        batched["mixed"]["error_vs_fp64"] = mixed_error(batched["fp64"].pop("results"),
+                                                        batched["mixed"].pop("results"))
 
     serving = None
     if not args.skip_serve and mixed:
@@ -392,8 +430,8 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": round(prof["max_ms"] / K, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"Sedov blast --s {s} --r {r} (b=1, c=1), plain double path, "
-                               "host TimeIncrement per cycle",
+        "config": {"workload": workload(s, r),
+                   "path": "plain double path (LULESH_FP64), host TimeIncrement per cycle",
                    "elements": ne, "nodes": nn, "mean_eos_rep": round(rep_avg, 3),
                    "parallelism": "replicas only (one independent problem per GPU)",
                    "l2": f"no flush: working set {lul.Batch.footprint('fp64', args.size) / 1e9:.2f} GB "
@@ -405,7 +443,8 @@ def run_ours(args) -> None:
         "gpu_launches": launches,
         "fom": fom(value),
         "kernel_ms_per_step": {k: round(v / K, 4) for k, v in prof["kernel_ms"].items()},
-        "roofline": roofline(prof, "fp64", ne, nn, rep_avg, fp64_peak, "measured live"),
+        "roofline": roofline(prof, "fp64", ne, nn, rep_avg, fp64_peak, "measured live",
+                             ms_per_step=prof["max_ms"] / K),
         "pipe_rates_per_s": {k: float(f"{v:.4g}") for k, v in rates.items()},
         "graph": {"value": round(gvalue, 1), "unit": UNIT,
                   "ms_per_step": round(gprof["max_ms"] / K, 4),
@@ -453,6 +492,9 @@ def run_batched(lul, precision: str, n: int, seed: int, tune: bool) -> dict:
     zc = sum(x["numElem"] * x["cycle"] for x in st)
     errs = sum(1 for x in st if x["err"] != 0)
     launches = b.launches - launches0
+    # per problem, in admission order: cycles run and final origin energy
+    # (computed on the device)
+    results = [(x["cycle"], b.verify(x["slot"])["e0"]) for x in sorted(st, key=lambda x: x["slot"])]
     b.close()
     # the same problems run one at a time through the single-problem path
     # (device-built handle, CUDA-graph time loop): device time
@@ -468,7 +510,7 @@ def run_batched(lul, precision: str, n: int, seed: int, tune: bool) -> dict:
            "cycles_min_max": [min(x["cycle"] for x in st), max(x["cycle"] for x in st)],
            "elements": sum(x["numElem"] for x in st), "errors": errs,
            "gpu_launches": launches, "admit_s": round(admit_s, 2),
-           "tuning": tuning,
+           "tuning": tuning, "results": results,
            "solo_device_s": round(solo_ms / 1e3, 3),
            "vs_solo_runs": round(solo_ms / total_ms, 3),
            "how": "all problems admitted into one pool, cycles replayed from one CUDA graph "
@@ -478,7 +520,21 @@ def run_batched(lul, precision: str, n: int, seed: int, tune: bool) -> dict:
     return out
 
 
-def run_serving(lul, n: int, seed: int, single_rate: float, budget_gb: float = 160.0) -> dict:
+def mixed_error(ref: list, mixed: list) -> dict:
+    """Relative e(0) error of mixed runs against double runs of the same
+    problems, and the count of problems whose cycle counts differ."""
+    import numpy as np
+
+    err = np.array([abs(m[1] - r[1]) / abs(r[1]) for r, m in zip(ref, mixed)])
+    return {"problems": len(err), "e0_rel_max": float(f"{err.max():.3g}"),
+            "e0_rel_p99": float(f"{np.quantile(err, 0.99):.3g}"),
+            "e0_rel_median": float(f"{np.median(err):.3g}"),
+            "above_1e-6": int((err > 1e-6).sum()),
+            "cycle_mismatches": sum(1 for r, m in zip(ref, mixed) if r[0] != m[0])}
+
+
+def run_serving(lul, n: int, seed: int, single_rate: float, budget_gb: float = 160.0,
+                check_max_s: int = 64) -> dict:
     """Serving workload: n requests with s uniform in [20, 120], regions in
     {11, 21}, energy x lognormal(0, 0.25), mixed precision, Poisson arrivals at
     twice the single-problem throughput, under a budget_gb HBM pool. The
@@ -498,6 +554,19 @@ def run_serving(lul, n: int, seed: int, single_rate: float, budget_gb: float = 1
             for a, b, c, d in zip(s, r, scale, arrivals)]
     results, st = lul.serve(reqs, "mixed", hbm_budget=int(budget_gb * (1 << 30)), max_slots=256,
                             sync_ms=20.0)
+    # the served (mixed) results against double runs of the same problems, for
+    # the requests with s <= check_max_s (one double batch, untimed)
+    pick = [i for i, q in enumerate(reqs) if q["s"] <= check_max_s]
+    need = sum(lul.Batch.footprint("fp64", reqs[i]["s"]) for i in pick)
+    b = lul.Batch("fp64", pool_bytes=int(need * 1.05) + (64 << 20), max_slots=max(len(pick), 1))
+    slots = [b.admit(s=reqs[i]["s"], nr=reqs[i]["nr"], energy_scale=reqs[i]["energy_scale"]) for i in pick]
+    while b.run(64)[0]:
+        pass
+    cyc = {x["slot"]: x["cycle"] for x in b.status()}
+    ref = [(cyc[sl], b.verify(sl)["e0"]) for sl in slots]
+    b.close()
+    check = mixed_error(ref, [(results[i]["cycles"], results[i]["e0"]) for i in pick])
+    check["requests_checked"] = f"the {len(pick)} requests with s <= {check_max_s}"
     return {"requests": n, "seed": seed, "arrival_rate_per_s": round(rate, 4),
             "budget_gb": budget_gb, "precision": "mixed",
             "p50_time_to_solution_s": round(st["p50_s"], 3), "p99_time_to_solution_s": round(st["p99_s"], 3),
@@ -505,6 +574,9 @@ def run_serving(lul, n: int, seed: int, single_rate: float, budget_gb: float = 1
             "value": round(st["zone_cycles_per_s"], 1), "unit": UNIT, "wall_s": round(st["wall_s"], 2),
             "device_s": round(st["device_s"], 2), "zone_cycles": st["zone_cycles"],
             "max_resident": st["max_resident"], "served": st["served"],
+            "peak_resident_gb": round(st["peak_resident_bytes"] / (1 << 30), 2),
+            "p50_queue_s": round(st["p50_queue_s"], 3), "p99_queue_s": round(st["p99_queue_s"], 3),
+            "error_vs_fp64": check,
             "errors": sum(1 for x in results if x["err"] != 0), "gpu_launches": st["launches"],
             "how": "lulesh_serve: arrived requests are admitted by HBM footprint, each built on the "
                    "device in its pool block, ~20 ms graph chunks replay every resident problem, each "
@@ -530,7 +602,8 @@ def run_reference(args) -> None:
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": K, "warmup": W, "ms_per_step": round(1e3 * secs / K, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"Sedov blast --s {s} --r {r} (b=1, c=1)", "elements": ne},
+        "config": {"workload": workload(s, r), "path": "the reference's CPU algorithm",
+                   "elements": ne},
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{K} cycles of s={s} r={r} after {W} warm-up cycles; the "
                                    "reference's algorithm as the bit-exact C oracle (the reference "
@@ -555,12 +628,16 @@ def main() -> None:
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--skip-serve", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--batch-problems", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=2024)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != world:
+        ap.error(f"--gpus {args.gpus} but WORLD_SIZE is {world}: launch N > 1 GPUs with "
+                 f"torch.distributed.run --nproc-per-node {args.gpus}")
     import oracle
 
     if not oracle.LIB_PATH.exists():

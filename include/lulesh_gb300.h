@@ -312,7 +312,10 @@ typedef struct lulesh_serve_stats {
     double zone_cycles_per_s;  /* all requests' zone-cycles / wall_s */
     double p50_s, p99_s, mean_s; /* time to solution */
     int64_t zone_cycles, launches;
-    int32_t served, max_resident;
+    int32_t served, max_resident; /* requests served; most problems resident at once */
+    int64_t peak_resident_bytes;  /* most pool bytes the resident problems held at once
+                                     (lulesh_batch_footprint each), against hbm_budget */
+    double p50_queue_s, p99_queue_s; /* admission delay (admitted - arrival) */
 } lulesh_serve_stats;
 
 int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_slots, const lulesh_request* reqs,
@@ -357,15 +360,21 @@ int lulesh_dev_profile_end(lulesh_dev* dev, lulesh_profile* out);
  * through its own pool or budget, or a loop that cannot afford cudaMalloc's
  * possible device-wide synchronization. From the caller's device arrays ss,
  * vdov and arealg (numElem each) it writes out_dt[0] = dtcourant and
- * out_dt[1] = dthydro (out_dt: 2 doubles of device memory) with the minima
- * lulesh_dev_step returns, using qqc and dvovmax of lulesh_params.
+ * out_dt[1] = dthydro (out_dt: 2 doubles of device memory), using qqc and
+ * dvovmax of lulesh_params: the minima lulesh_dev_step returns for the same
+ * arrays on a LULESH_FP64 or LULESH_MIXED handle, bit for bit (the same
+ * arithmetic), and within about one ulp of a LULESH_FP64_EXACT handle's
+ * (whose divide and square root are IEEE). Values are folded with fmin, so
+ * any finite input works and NaN candidates are ignored.
  * Asynchronous on `stream` (a cudaStream_t; NULL = the legacy default stream).
  * Working memory is one file-scope device array of 256 KiB that every GPU
  * loading this library keeps until exit; it bounds numElem to
- * LULESH_NOALLOC_MAX_ELEMS and larger sizes return LULESH_EINVAL. The first
- * call on a device looks up that array's device address once (call it before
- * any stream capture). Calls share the array: calls whose kernels overlap on
- * the GPU race and must be serialized by the caller. */
+ * LULESH_NOALLOC_MAX_ELEMS and larger sizes return LULESH_EINVAL. Each call
+ * whose stream is not capturing looks up that array's device address (so it
+ * follows a device reset); a call during stream capture reuses the last
+ * address, so the first call on a device must come before any capture
+ * (LULESH_EINVAL otherwise). Calls share the array: calls whose kernels
+ * overlap on the GPU race and must be serialized by the caller. */
 #define LULESH_NOALLOC_MAX_ELEMS 4194304
 int lulesh_dt_constraints_noalloc(const double* ss, const double* vdov, const double* arealg,
                                   int32_t numElem, double qqc, double dvovmax, double* out_dt,
@@ -374,21 +383,6 @@ int lulesh_dt_constraints_noalloc(const double* ss, const double* vdov, const do
 /* Page-locks (pin = 1) or releases (pin = 0) the host arrays of a Domain so
  * lulesh_leapfrog's per-cycle copies run at full link bandwidth. */
 int lulesh_domain_pin(lulesh_domain* d, int32_t pin);
-
-/* Measures the current GPU's pipe rates (no counterpart in the reference):
- * out[0] double FMA/s, out[1] double add/s, out[2] double divide/s,
- * out[3] double square root/s, out[4] float FMA/s (per-thread operations).
- * The double path is bound by out[0]; takes about 50 ms. */
-int lulesh_probe_pipe_rates(double out[5]);
-
-/* Evaluates one arithmetic helper of the fast variants on the device for n
- * inputs (no counterpart in the reference; accuracy tests compare the results
- * with correctly rounded host values): fn 0 reciprocal, 1 reciprocal cube
- * root, 2 square root, 3 reciprocal square root (inputs positive and normal
- * for 1-3), 4 the hardware seed of the reciprocal; 5 the mixed variant's
- * double-to-float rounding, 6 and 7 the high and low floats of its float-pair
- * split (results returned as doubles). n <= 2^26. */
-int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n);
 
 /* Selects the CUDA device used by handles created afterwards on this thread. */
 int lulesh_set_device(int32_t device);

@@ -107,7 +107,8 @@ class ServeStats(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("wall_s", "device_s", "zone_cycles_per_s", "p50_s", "p99_s",
                                           "mean_s")] + \
                [("zone_cycles", C.c_int64), ("launches", C.c_int64), ("served", C.c_int32),
-                ("max_resident", C.c_int32)]
+                ("max_resident", C.c_int32), ("peak_resident_bytes", C.c_int64), ("p50_queue_s", C.c_double),
+                ("p99_queue_s", C.c_double)]
 
 
 class DomainView(C.Structure):
@@ -161,8 +162,6 @@ def library() -> C.CDLL:
         "lulesh_dev_profile_end": (i32, [vp, C.POINTER(Profile)]),
         "lulesh_domain_pin": (i32, [vp, i32]),
         "lulesh_set_device": (i32, [i32]),
-        "lulesh_probe_pipe_rates": (i32, [C.POINTER(dbl)]),
-        "lulesh_probe_math": (i32, [i32, C.POINTER(dbl), C.POINTER(dbl), i64]),
         "lulesh_batch_create": (i32, [i32, C.c_uint64, i32, C.POINTER(vp)]),
         "lulesh_batch_destroy": (None, [vp]),
         "lulesh_batch_footprint": (i32, [i32, i32, C.POINTER(C.c_uint64)]),
@@ -411,10 +410,31 @@ def set_device(device: int) -> None:
     _check(library().lulesh_set_device(device), "lulesh_set_device")
 
 
+_probe_lib = None
+PROBE_LIB_PATH = HERE / "liblulesh_probe.so"
+
+
+def probe_library() -> C.CDLL:
+    """Loads liblulesh_probe.so, the measurement probes (not part of the
+    step's C ABI; the benchmark and the accuracy tests use it)."""
+    global _probe_lib
+    if _probe_lib is None:
+        if not PROBE_LIB_PATH.exists():
+            raise RuntimeError(f"{PROBE_LIB_PATH} is not built: run __graft_entry__.build()")
+        lib = C.CDLL(str(PROBE_LIB_PATH))
+        lib.lulesh_probe_pipe_rates.restype = C.c_int32
+        lib.lulesh_probe_pipe_rates.argtypes = [C.POINTER(C.c_double)]
+        lib.lulesh_probe_math.restype = C.c_int32
+        lib.lulesh_probe_math.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                          C.c_int64]
+        _probe_lib = lib
+    return _probe_lib
+
+
 def pipe_rates() -> dict:
     """Measured double FMA/add/divide/sqrt and float FMA rates (ops/s) of the current GPU."""
     out = (C.c_double * 5)()
-    _check(library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
+    _check(probe_library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
     return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma"), list(out)))
 
 
@@ -429,7 +449,7 @@ def probe_math(fn: str, x):
 
     xs = np.ascontiguousarray(x, dtype=np.float64)
     out = np.empty_like(xs)
-    _check(library().lulesh_probe_math(MATH_FUNCTIONS[fn], xs.ctypes.data_as(C.POINTER(C.c_double)),
+    _check(probe_library().lulesh_probe_math(MATH_FUNCTIONS[fn], xs.ctypes.data_as(C.POINTER(C.c_double)),
                                        out.ctypes.data_as(C.POINTER(C.c_double)), xs.size),
            "lulesh_probe_math")
     return out

@@ -1,8 +1,9 @@
 """In-tree build of the GB300 LULESH library and command-line driver.
 
 Compiles every translation unit under csrc/ for sm_103a with nvcc (in
-parallel), links liblulesh_gb300.so next to this file and the lulesh-gb300
-executable (the reference's command line on top of the C ABI).
+parallel), links liblulesh_gb300.so next to this file, the lulesh-gb300
+executable (the reference's command line on top of the C ABI) and
+liblulesh_probe.so (measurement probes for the benchmark and tests only).
 
 Floating-point contraction is part of the numerics contract:
   * fp64_exact.cu, time_increment.cu, verify.cu and device_init.cu are
@@ -43,11 +44,18 @@ UNITS = [
     ("device_init.cu", ["--fmad=false"]),
     ("capi.cu", []),
     ("noalloc.cu", []),
-    ("probe.cu", []),
     ("batch.cu", []),
     ("serve.cu", []),
     ("domain.cpp", ["-x", "cu", "--fmad=false"]),
 ]
+# The measurement probes (pipe rates, the fast helpers' accuracy) form their
+# own library for the benchmark and the accuracy tests; the product library
+# does not contain them.
+PROBE_UNITS = [
+    ("probe.cu", []),
+    ("probe_math.cu", []),
+]
+PROBE_LIB = HERE / "liblulesh_probe.so"
 
 
 def nvcc() -> str:
@@ -76,13 +84,14 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     cc = nvcc()
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "lulesh_gb300.h"]
     jobs = []
-    objs = []
-    for src, extra in UNITS:
-        s = CSRC / src
-        o = BUILD / (src + ".o")
-        objs.append(o)
-        if force or _stale(o, [s] + headers):
-            jobs.append([cc, *NVCC_COMMON, *extra, "-c", str(s), "-o", str(o)])
+    objs, probe_objs = [], []
+    for units, out in ((UNITS, objs), (PROBE_UNITS, probe_objs)):
+        for src, extra in units:
+            s = CSRC / src
+            o = BUILD / (src + ".o")
+            out.append(o)
+            if force or _stale(o, [s] + headers):
+                jobs.append([cc, *NVCC_COMMON, *extra, "-c", str(s), "-o", str(o)])
     with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         for cmd in jobs:
             if verbose:
@@ -90,6 +99,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB, objs):
         _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lpthread"])
+    if force or jobs or _stale(PROBE_LIB, probe_objs):
+        _run([cc, *ARCH, "-shared", "-o", str(PROBE_LIB), *map(str, probe_objs), "-lcudart"])
     drv = CSRC / "driver.cpp"
     if drv.exists() and (force or _stale(EXE, [drv, LIB] + headers)):
         _run([cc, *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-ffp-contract=off", f"-I{ROOT / 'include'}",

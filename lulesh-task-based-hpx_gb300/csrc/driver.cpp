@@ -2,8 +2,10 @@
 // the GB300 C ABI.
 //
 // Flags as the reference registers them (lulesh.cc:2421-2432): --s --r --i
-// --b --c --q --p (plus --f/--v, accepted and ignored: viz output is not
-// built), and --hpx:threads=N is accepted for drop-in command lines. Added:
+// --b --c --q --p, --f (accepted and ignored: it only sets the number of viz
+// files) and --v, refused as the reference refuses it when built without viz
+// output (lulesh-util.cc:48-54: message and exit(-1)); Silo viz output is not
+// built here. --hpx:threads=N is accepted for drop-in command lines. Added:
 // --precision fp64|fp64_exact|mixed and --graph (device TimeIncrement with
 // the cycle replayed from a CUDA graph).
 //
@@ -51,7 +53,10 @@ int main(int argc, char** argv) {
         }
         if (a == "--q") { quiet = 1; continue; }
         if (a == "--p") { prog = 1; continue; }
-        if (a == "--v") continue;
+        if (a == "--v") {
+            std::printf("Use of --v requires a build with viz output (Silo), which this build does not have\n");
+            return -1;
+        }
         if (a == "--graph") { graph = 1; continue; }
         if (!has_inline && i + 1 >= argc) {
             std::fprintf(stderr, "option %s needs a value\n", a.c_str());

@@ -119,8 +119,6 @@ int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
 int launch_material(const Mesh& m, cudaStream_t s);
 // matOrder positions [first, end); accumulate: fold the dt minima into m.result's
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
-// the fast helpers on n inputs (probe.cu's lulesh_probe_math)
-int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t s);
 // the resident loop's form: kinematics that also stores the element geometry
 // of the updated coordinates (m.geo), forces that read it, and the pass that
 // forms it from the current coordinates when it is stale
@@ -152,8 +150,6 @@ int launch_material(const Mesh& m, cudaStream_t s);
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
 int launch_mirror(const Mesh& m, cudaStream_t s);
 int launch_mirror_range(const Mesh& m, int first, int end, cudaStream_t s);  // nodes [first, end)
-// the float conversions on n inputs (probe.cu's lulesh_probe_math)
-int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t s);
 }  // namespace mixed
 
 // Device-side TimeIncrement for the graph form (time_increment.cu).

@@ -22,6 +22,7 @@
 #define LULESH_EXACT 0
 #define LULESH_FLOAT_Q 1
 #include "step_math.cuh"
+#include "float_pair.cuh"
 
 namespace lulesh {
 namespace mixed {
@@ -33,27 +34,6 @@ __device__ __forceinline__ void rel8(const float2* __restrict__ p, const int nl[
     for (int k = 0; k < 8; ++k) a[k] = __ldg(p + nl[k]);
 #pragma unroll
     for (int k = 0; k < 8; ++k) r[k] = (a[k].x - a[0].x) + (a[k].y - a[0].y);
-}
-
-// The float-pair mirror of v, (hi, lo) = (fl(v), fl(v - hi)) with fl the
-// round-to-nearest-even conversion, on the integer pipe (narrow's rounding of
-// the bit pattern; v - hi is one exact double subtraction). Bit for bit the
-// conversions' result for |v| in [2^-74, float's largest], where lo is zero
-// or a normal float; zeros map to zeros and other values take the conversion
-// instructions out of line.
-__device__ __noinline__ float2 split_convert(double v) {
-    const float hi = __double2float_rn(v);
-    return make_float2(hi, __double2float_rn(v - double(hi)));
-}
-
-__device__ __forceinline__ float2 split(double v) {
-    const unsigned long long b = __double_as_longlong(v);
-    const unsigned e = unsigned(b >> 52) & 0x7ffu;
-    if ((b << 1) == 0ull) return make_float2(__uint_as_float(unsigned(b >> 32)), 0.0f);  // +-0
-    if (e < 949u || e > 1150u) return split_convert(v);
-    const unsigned long long hb = round_to_float_bits(b);
-    const unsigned long long lb = __double_as_longlong(v - __longlong_as_double(hb));
-    return make_float2(float_from_rounded(hb), (lb << 1) == 0ull ? 0.0f : float_from_rounded(round_to_float_bits(lb)));
 }
 
 __device__ __forceinline__ void mirror_node(const Mesh& m, int n) {
@@ -271,24 +251,6 @@ int launch_material(const Mesh& m, cudaStream_t s) {
 }
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s) {
     k_material<<<m.matGrid, kMatBlock, 0, s>>>(m, first, end, accumulate ? 1 : 0);
-    return 1;
-}
-
-// The integer-pipe conversions evaluated on given inputs, for tests against
-// the host's round-to-nearest-even float conversion. fn: 5 narrow, 6 and 7
-// the high and low float of split (each returned as the double it equals).
-__global__ void k_math_probe(int fn, const double* __restrict__ in, double* __restrict__ out, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double x = in[i];
-    float r;
-    if (fn == 5) r = narrow(x);
-    else if (fn == 6) r = split(x).x;
-    else r = split(x).y;
-    out[i] = double(r);
-}
-int launch_math_probe(int fn, const double* in, double* out, int n, cudaStream_t s) {
-    k_math_probe<<<blocks_for(n, 256), 256, 0, s>>>(fn, in, out, n);
     return 1;
 }
 

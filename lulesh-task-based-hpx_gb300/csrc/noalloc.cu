@@ -44,9 +44,16 @@ __global__ void __launch_bounds__(kBlock)
                      unsigned char* scratch, double* out) {
     DtPartial* partials = reinterpret_cast<DtPartial*>(scratch);
     unsigned* counter = reinterpret_cast<unsigned*>(scratch + kCounterOffset);
+    // fmin folds (not the step's bit-pattern minimum, which assumes the
+    // non-negative candidates of its own state): caller arrays may hold any
+    // value, and a NaN candidate is then ignored as fmin ignores it
     double dtc = 1.0e+20, dth = 1.0e+20;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dt_constraints(prm, __ldg(ss + i), __ldg(vdov + i), __ldg(arealg + i), dtc, dth);
+    double courant, hydro;
+    if (i < n && dt_candidates(prm, __ldg(ss + i), __ldg(vdov + i), __ldg(arealg + i), courant, hydro)) {
+        dtc = fmin(dtc, courant);
+        dth = fmin(dth, hydro);
+    }
     block_min2(dtc, dth);
     __shared__ bool last;
     if (threadIdx.x == 0) {
@@ -71,19 +78,27 @@ __global__ void __launch_bounds__(kBlock)
     }
 }
 
-// Device address of g_dt_scratch for each device, looked up once per device
-// (with that device current) on the first call there.
+// Device address of g_dt_scratch for each device (looked up with that device
+// current). Host code cannot pass g_dt_scratch itself: its name there is a
+// host-side stand-in, not a device address. The address is looked up again
+// on every call whose stream is not capturing, so it follows a device reset
+// (which may reload the module elsewhere); a call made while its stream
+// captures a graph uses the address of the last call on that device, so the
+// first call on a device must come before any capture.
 static std::mutex g_mutex;
 static void* g_addr[64] = {};
 
-static int scratch_address(int device, void** out) {
+static int scratch_address(int device, cudaStream_t stream, void** out) {
     if (device < 0 || device >= 64) return LULESH_EINVAL;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) return LULESH_ECUDA;
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_addr[device]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_dt_scratch) != cudaSuccess || !p) return LULESH_ECUDA;
         g_addr[device] = p;
     }
+    if (!g_addr[device]) return LULESH_EINVAL;  // first call on this device inside a capture
     *out = g_addr[device];
     return LULESH_OK;
 }
@@ -99,11 +114,11 @@ extern "C" int lulesh_dt_constraints_noalloc(const double* ss, const double* vdo
     if (numElem > LULESH_NOALLOC_MAX_ELEMS) return LULESH_EINVAL;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return LULESH_ECUDA;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     void* base = nullptr;
-    const int st = scratch_address(device, &base);
+    const int st = scratch_address(device, s, &base);
     if (st != LULESH_OK) return st;
     unsigned char* scratch = static_cast<unsigned char*>(base);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(scratch + kCounterOffset, 0, sizeof(unsigned), s) != cudaSuccess)
         return LULESH_ECUDA;
     lulesh_params prm{};

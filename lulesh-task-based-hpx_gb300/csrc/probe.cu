@@ -1,6 +1,7 @@
-// Pipe-rate probe: the double FMA, add, divide and square-root throughput and
-// the float FMA throughput of the current GPU, for the FP64 roof that bounds
-// the double-precision step (bench.py reports kernel rates against it).
+// Pipe-rate probe (liblulesh_probe.so, not the product library): the double
+// FMA, add, divide and square-root throughput and the float FMA throughput of
+// the current GPU, for the FP64 roof that bounds the double-precision step
+// (the benchmark reports kernel rates against it).
 //
 // Each thread runs 8 independent dependency chains of one operation in a
 // loop; the grid is 8 blocks of 256 threads per SM. Rates are operations per
@@ -8,7 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "lulesh_gb300.h"
-#include "lulesh_dev.h"
+#include "lulesh_probe.h"
 
 namespace {
 
@@ -83,28 +84,5 @@ extern "C" int lulesh_probe_pipe_rates(double out[5]) {
     cudaEventDestroy(e1);
     cudaFree(buf);
     if (cudaGetLastError() != cudaSuccess) st = LULESH_ECUDA;
-    return st;
-}
-
-extern "C" int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n) {
-    if (!in || !out || fn < 0 || fn > 7 || n < 1 || n > (int64_t(1) << 26)) return LULESH_EINVAL;
-    const size_t bytes = sizeof(double) * size_t(n);
-    double *d_in = nullptr, *d_out = nullptr;
-    if (cudaMalloc(&d_in, bytes) != cudaSuccess) return LULESH_ENOMEM;
-    if (cudaMalloc(&d_out, bytes) != cudaSuccess) {
-        cudaFree(d_in);
-        return LULESH_ENOMEM;
-    }
-    int st = LULESH_OK;
-    if (cudaMemcpy(d_in, in, bytes, cudaMemcpyHostToDevice) != cudaSuccess) st = LULESH_ECUDA;
-    if (st == LULESH_OK) {
-        if (fn <= 4) lulesh::fp64::launch_math_probe(fn, d_in, d_out, int(n), nullptr);
-        else lulesh::mixed::launch_math_probe(fn, d_in, d_out, int(n), nullptr);
-        if (cudaGetLastError() != cudaSuccess ||
-            cudaMemcpy(out, d_out, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
-            st = LULESH_ECUDA;
-    }
-    cudaFree(d_in);
-    cudaFree(d_out);
     return st;
 }

@@ -65,7 +65,9 @@ extern "C" int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_
     std::deque<int> pending;      // arrived, waiting for a slot and pool memory
     std::map<int, int> inflight;  // slot -> request
     std::vector<lulesh_slot_status> status(max_slots);
+    std::map<int, uint64_t> slot_bytes;  // slot -> pool bytes of its problem
     int done = 0, chunk = 8, max_resident = 0;
+    uint64_t resident_bytes = 0, peak_bytes = 0;
     double device_ms = 0.0;
     while (st == LULESH_OK && done < n) {
         const double t = now_s();
@@ -85,10 +87,15 @@ extern "C" int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_
             }
             results[*it].admitted_s = now_s();
             inflight[slot] = *it;
+            uint64_t need = 0;
+            lulesh_batch_footprint(precision, reqs[*it].problem.s, &need);
+            slot_bytes[slot] = need;
+            resident_bytes += need;
             it = pending.erase(it);
         }
         if (st != LULESH_OK) break;
         max_resident = std::max(max_resident, int(inflight.size()));
+        peak_bytes = std::max(peak_bytes, resident_bytes);
         if (inflight.empty()) {
             // nothing resident (every request fits the empty pool, so none is
             // pending): sleep until the next arrival, in short steps
@@ -128,6 +135,8 @@ extern "C" int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_
             r.maxrel = vr.maxrel;
             if (st == LULESH_OK) st = lulesh_batch_retire(b, it->first);
             if (st != LULESH_OK) break;
+            resident_bytes -= slot_bytes[it->first];
+            slot_bytes.erase(it->first);
             it = inflight.erase(it);
             ++done;
         }
@@ -137,11 +146,12 @@ extern "C" int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_
     if (st != LULESH_OK) return st;
 
     if (stats) {
-        std::vector<double> tts(n);
+        std::vector<double> tts(n), queued(n);
         double last = 0.0;
         int64_t zc = 0;
         for (int i = 0; i < n; ++i) {
             tts[i] = results[i].time_to_solution_s;
+            queued[i] = results[i].admitted_s - results[i].arrival_s;
             last = std::max(last, results[i].finished_s);
             zc += results[i].zone_cycles;
         }
@@ -156,6 +166,9 @@ extern "C" int lulesh_serve(int32_t precision, uint64_t hbm_budget, int32_t max_
         stats->launches = launches;
         stats->served = done;
         stats->max_resident = max_resident;
+        stats->peak_resident_bytes = int64_t(peak_bytes);
+        stats->p50_queue_s = quantile(queued, 0.50);
+        stats->p99_queue_s = quantile(queued, 0.99);
     }
     return LULESH_OK;
 }

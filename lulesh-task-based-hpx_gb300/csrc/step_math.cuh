@@ -1200,17 +1200,27 @@ __device__ __forceinline__ double eos_element(const Mesh& m, int i, double vnewc
     return m.prm.refdens == 1.0 ? eos_body<true>(m, i, vnewc, rep) : eos_body<false>(m, i, vnewc, rep);
 }
 
-// Courant and hydro constraints of one element (lulesh.cc:1938-1974),
-// folded into running minima; vdov == 0 elements do not constrain.
-__device__ __forceinline__ void dt_constraints(const lulesh_params& P, double ss, double vdov,
-                                               double arealg, double& dtc, double& dth) {
-    if (f_is_zero(vdov)) return;
+// Courant and hydro candidates of one element (lulesh.cc:1938-1974); false
+// where vdov == 0 (the element does not constrain).
+__device__ __forceinline__ bool dt_candidates(const lulesh_params& P, double ss, double vdov,
+                                              double arealg, double& courant, double& hydro) {
+    if (f_is_zero(vdov)) return false;
     const double qqc2 = 64.0 * P.qqc * P.qqc;
     double dtf = ss * ss;
     if (f_lt(vdov, 0.0)) dtf += qqc2 * arealg * arealg * vdov * vdov;
-    dtf = div_sqrt(arealg, dtf);  // arealg / sqrt(dtf)
-    dtc = nonneg_min(dtc, dtf);
-    dth = nonneg_min(dth, quot(P.dvovmax, fabs(vdov) + 1.e-20));
+    courant = div_sqrt(arealg, dtf);  // arealg / sqrt(dtf)
+    hydro = quot(P.dvovmax, fabs(vdov) + 1.e-20);
+    return true;
+}
+
+// The same constraints folded into running minima (the candidates of the
+// step's own state are non-negative: ss, arealg >= 0).
+__device__ __forceinline__ void dt_constraints(const lulesh_params& P, double ss, double vdov,
+                                               double arealg, double& dtc, double& dth) {
+    double courant, hydro;
+    if (!dt_candidates(P, ss, vdov, arealg, courant, hydro)) return;
+    dtc = nonneg_min(dtc, courant);
+    dth = nonneg_min(dth, hydro);
 }
 
 // Block-wide min of (a, b); the result is valid in thread 0.

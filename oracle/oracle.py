@@ -20,7 +20,17 @@ HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "liblulesh_oracle.so"
 CLI_PATH = HERE / "lulesh-oracle"
 REF_BIN = HERE / "_ref" / "lulesh-ref"
-REF_SOURCES = Path("/root/reference")
+
+
+def _ref_sources() -> Path:
+    """The reference checkout the recipe builds from (LULESH_REF_DIR, else the
+    default oracle/Makefile names)."""
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", str(HERE), "print-ref-dir"],
+                       capture_output=True, text=True)
+    return Path(r.stdout.strip() or "/nonexistent")
+
+
+REF_SOURCES = _ref_sources()
 
 NODE_FIELDS = ("x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy", "fz")
 ELEM_FIELDS = ("e", "p", "q", "ql", "qq", "v", "vnew", "delv", "vdov", "arealg", "ss")

@@ -53,6 +53,9 @@ def test_each_request_equals_its_solo_run(lulesh, precision):
         assert res["zone_cycles"] == req["s"] ** 3 * n
     assert 0 < stats["p50_s"] <= stats["p99_s"]
     assert stats["zone_cycles"] == sum(r["zone_cycles"] for r in results)
+    # admission by footprint: the resident problems never held more than the budget
+    assert 0 < stats["peak_resident_bytes"] <= budget
+    assert 0 <= stats["p50_queue_s"] <= stats["p99_queue_s"]
 
 
 def test_request_larger_than_the_budget_is_refused(lulesh):

@@ -17,8 +17,8 @@ from conftest import ROOT, gpu_available
 HEADER = ROOT / "include" / "lulesh_gb300.h"
 
 
-def declared_functions() -> list[str]:
-    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+def declared_functions(header=HEADER) -> list[str]:
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
     return sorted(set(re.findall(r"\b(lulesh_[a-z0-9_]+)\s*\(", text)))
 
 
@@ -28,6 +28,20 @@ def test_library_exports_every_declared_symbol(lulesh):
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_probes_live_in_their_own_library(lulesh):
+    """The measurement probes are not part of the step's ABI: the product
+    library does not export them, liblulesh_probe.so exports what its header
+    declares."""
+    probe_header = ROOT / "lulesh-task-based-hpx_gb300" / "csrc" / "lulesh_probe.h"
+    names = declared_functions(probe_header)
+    assert names == ["lulesh_probe_math", "lulesh_probe_pipe_rates"]
+    plib = lulesh.probe_library()
+    assert all(hasattr(plib, n) for n in names)
+    product = C.CDLL(str(lulesh.LIB_PATH))
+    assert not any(hasattr(product, n) for n in names)
+    assert not set(names) & set(declared_functions())
 
 
 @pytest.mark.parametrize("s,r,b,c", [(5, 11, 1, 1), (9, 21, 1, 2), (8, 1, 1, 1), (7, 16, 2, 3)])
@@ -187,3 +201,15 @@ def test_largest_problem_size(lulesh):
         with pytest.raises(lulesh.LuleshError) as ei:
             call()
         assert ei.value.status == lulesh.EINVAL
+
+
+def test_driver_refuses_viz_flag(lulesh):
+    """The reference refuses -v when built without viz output
+    (lulesh-util.cc:48-54: a message and exit(-1)); the driver does the same
+    before any device work, so it needs no GPU."""
+    import subprocess
+
+    exe = ROOT / "lulesh-task-based-hpx_gb300" / "lulesh-gb300"
+    r = subprocess.run([str(exe), "--s", "5", "--v"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 255  # exit(-1)
+    assert "requires a build with viz output" in r.stdout

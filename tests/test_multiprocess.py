@@ -92,13 +92,22 @@ def test_roofline_arithmetic():
     ne, nn, cycles = 3_375_000, 3_442_951, 10
     prof = {"kernel_ms": {"forces": 42.6, "nodes": 2.4, "kinematics": 20.6, "material": 14.7},
             "cycles": cycles}
-    rl = bench.roofline(prof, "fp64", ne, nn, 3.26, fp64_peak=1.2, fp64_kind="test")
+    rl = bench.roofline(prof, "fp64", ne, nn, 3.26, fp64_peak=1.2, fp64_kind="test", ms_per_step=8.5)
     assert rl["kernel"] == "forces" and rl["bound"] == "hbm" and rl["unit"] == "GB/s"
     launch_s = 42.6 / cycles / 1e3
     assert rl["avg_launch_ms"] == pytest.approx(4.26)
-    assert rl["bytes_per_launch"] == bench.BYTES_PER_UNIT["fp64"]["forces"] * ne
+    # the algorithmic bytes of the four-kernel step: 320 per element for forces
+    assert bench.BYTES_PER_UNIT["fp64"]["forces"] == 320
+    assert sum(bench.BYTES_PER_UNIT["fp64"].values()) == bench.STEP_BYTES_PER_ZONE_CYCLE["fp64"] == 1020
+    assert sum(bench.BYTES_PER_UNIT["mixed"].values()) == bench.STEP_BYTES_PER_ZONE_CYCLE["mixed"] == 780
+    assert rl["bytes_per_launch"] == 320 * ne
     assert rl["achieved"] == pytest.approx(rl["bytes_per_launch"] / launch_s / 1e9, rel=1e-3)
     assert rl["frac"] == pytest.approx(rl["achieved"] / rl["peak"], rel=1e-3)
+    lay = bench.LAYOUT_BYTES_PER_UNIT["fp64"]["forces"] * ne / launch_s / 1e9
+    assert rl["frac_layout"] == pytest.approx(lay / rl["peak"], rel=1e-3)
+    step_gbs = 1020 * ne / 8.5e-3 / 1e9
+    assert rl["step"]["achieved"] == pytest.approx(step_gbs, rel=1e-3)
+    assert rl["step"]["frac"] == pytest.approx(step_gbs / rl["peak"], rel=1e-3)
     assert rl["traffic"] == bench.TRAFFIC_PER_UNIT["fp64"]["forces"] * ne
     fp = rl["fp64_pipe"]
     rate = bench.FP64_INSTR_PER_UNIT["fp64"]["forces"] * ne / launch_s
@@ -122,3 +131,26 @@ def test_fom_matches_reference_report_formula():
     grind = elapsed_s * 1e6 / cycles / elements
     assert f["grind_time_us_per_zone_cycle"] == pytest.approx(grind, rel=1e-5)
     assert f["fom"] == pytest.approx(1000.0 / grind, rel=1e-5)
+
+
+def test_mixed_error_summary():
+    """bench.mixed_error: relative e(0) error of mixed runs against double runs
+    of the same problems, and the cycle-count mismatches."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    ref = [(100, 2.0), (200, 4.0), (300, 1.0)]
+    mixed = [(100, 2.0 * (1 + 1e-8)), (201, 4.0 * (1 - 3e-6)), (300, 1.0)]
+    d = bench.mixed_error(ref, mixed)
+    assert d["problems"] == 3 and d["cycle_mismatches"] == 1 and d["above_1e-6"] == 1
+    assert d["e0_rel_max"] == pytest.approx(3e-6, rel=1e-3)
+    assert d["e0_rel_median"] == pytest.approx(1e-8, rel=1e-3)
+
+
+def test_gpus_flag_must_match_world_size():
+    """bench.py --gpus N without N launched ranks is refused, not run as one replica."""
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--skip-cpu"],
+                       capture_output=True, text=True, timeout=120, cwd=ROOT,
+                       env={k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK")})
+    assert r.returncode != 0
+    assert "WORLD_SIZE is 1" in r.stderr

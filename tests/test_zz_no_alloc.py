@@ -7,7 +7,8 @@ synchronization. Its only working memory is a fixed 256 KiB array inside the
 library. These tests call it through the C ABI on device arrays owned by the
 caller (torch tensors here) and check both minima against what the existing
 entry point, lulesh_dev_step, returns for the same state, on two cycles in a
-row; they also check that sizes above LULESH_NOALLOC_MAX_ELEMS are refused.
+row (bit for bit, on a double and a mixed handle), run it at its size limit,
+and check that sizes above LULESH_NOALLOC_MAX_ELEMS are refused.
 
 This file is collected last on purpose, so a run that stops at the first
 failure has already run every other test.
@@ -42,13 +43,14 @@ def _host_minima(ss, vdov, arealg, qqc, dvovmax, n):
     return dtc, dth
 
 
-def test_noalloc_minima_match_step_on_consecutive_cycles(lulesh):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_noalloc_minima_match_step_on_consecutive_cycles(lulesh, precision):
     torch = pytest.importorskip("torch")
     lulesh.set_device(0)
     torch.cuda.set_device(0)
     fn = _bind(lulesh.library())
     dom = lulesh.HostDomain(20, 11, 1, 1)
-    dev = lulesh.Device(dom, "fp64")
+    dev = lulesh.Device(dom, precision)
     assert dev.run(40) == 40  # let the blast spread over many elements
     prm = dom.view.params
     out = torch.full((2,), -1.0, dtype=torch.float64, device="cuda")
@@ -66,14 +68,52 @@ def test_noalloc_minima_match_step_on_consecutive_cycles(lulesh):
         assert st == 0
         torch.cuda.synchronize()
         got = out.cpu().numpy()
-        assert got[0] == pytest.approx(dtc, rel=1e-13)
-        assert got[1] == pytest.approx(dth, rel=1e-13)
-        # a smaller size right after: the counter is cleared per call
+        # the same per-element arithmetic as the step's material kernel, and
+        # exact minima: equal bit for bit
+        assert got[0] == dtc
+        assert got[1] == dth
+        # a smaller size right after: the counter is cleared per call. The
+        # host minima use correctly rounded divide and square root, the
+        # device its reciprocal forms (within about one ulp).
         n = dom.numElem // 3
         assert fn(ss.data_ptr(), vdov.data_ptr(), arealg.data_ptr(), n, prm.qqc, prm.dvovmax,
                   out.data_ptr(), None) == 0
         torch.cuda.synchronize()
         want = _host_minima(dom.ss, dom.vdov, dom.arealg, prm.qqc, prm.dvovmax, n)
+        got = out.cpu().numpy()
+        assert got[0] == pytest.approx(want[0], rel=1e-13)
+        assert got[1] == pytest.approx(want[1], rel=1e-13)
+
+
+def test_noalloc_at_its_size_limit(lulesh):
+    """numElem = LULESH_NOALLOC_MAX_ELEMS fills every partial slot of the
+    fixed scratch: the smallest Courant candidate sits in the last element
+    and the smallest hydro candidate in block 0, and both must come out, on
+    two calls in a row."""
+    torch = pytest.importorskip("torch")
+    lulesh.set_device(0)
+    torch.cuda.set_device(0)
+    fn = _bind(lulesh.library())
+    n = MAX_ELEMS
+    rng = np.random.default_rng(11)
+    ss = rng.uniform(1.0, 2.0, n)
+    arealg = rng.uniform(0.5, 1.0, n)
+    vdov = rng.uniform(-1.0, 1.0, n)
+    vdov[rng.integers(0, n, 1000)] = 0.0  # elements that do not constrain
+    arealg[n - 1], ss[n - 1], vdov[n - 1] = 1e-3, 1.0, -1e-3  # smallest Courant
+    vdov[17] = 50.0  # largest |vdov| in block 0: smallest hydro
+    qqc, dvovmax = 2.0, 0.1
+    want = _host_minima(ss, vdov, arealg, qqc, dvovmax, n)
+    assert want[0] == pytest.approx(arealg[n - 1] / np.sqrt(ss[n - 1] ** 2 + 256 * 1e-6 * 1e-6))
+    assert want[1] == pytest.approx(dvovmax / 50.0)
+    d = [torch.from_numpy(a).cuda() for a in (ss, vdov, arealg)]
+    out = torch.full((2,), -1.0, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        out.fill_(-1.0)
+        torch.cuda.synchronize()
+        assert fn(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), n, qqc, dvovmax,
+                  out.data_ptr(), None) == 0
+        torch.cuda.synchronize()
         got = out.cpu().numpy()
         assert got[0] == pytest.approx(want[0], rel=1e-13)
         assert got[1] == pytest.approx(want[1], rel=1e-13)
