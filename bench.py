@@ -81,19 +81,18 @@ LAYOUT_BYTES_PER_UNIT = {
     "fp64": {"forces": 680, "nodes": 381, "kinematics": 568, "material": 204},
     "mixed": {"forces": 224, "nodes": 333, "kinematics": 184, "material": 180},
 }
-# DRAM bytes (read + write) per unit measured by ncu at s=100, where every
-# array exceeds L2; scaled by units per launch.
+# DRAM bytes (read + write) and FP64-pipe instructions (thread level:
+# sm__inst_executed_pipe_fp64 x 32) per unit, measured by ncu on this
+# workload (s=150 r=21, the second and third cycles); every array a kernel
+# streams is larger than L2. The material kernel's count depends on the
+# state (EOS passes, compressing elements); these are early cycles of the run.
 TRAFFIC_PER_UNIT = {
-    "fp64": {"forces": 648, "nodes": 342, "kinematics": 506, "material": 183},
-    "mixed": {"forces": 188, "nodes": 275, "kinematics": 157, "material": 149},
+    "fp64": {"forces": 672, "nodes": 368, "kinematics": 550, "material": 227},
+    "mixed": {"forces": 215, "nodes": 314, "kinematics": 177, "material": 198},
 }
-# FP64-pipe instructions per unit (thread level: sm__inst_executed_pipe_fp64
-# x 32 / units) measured by ncu at s=100 for the branch-free kernels; the
-# material kernel's count depends on the state (EOS repeats, compressing
-# elements), so it has none here.
 FP64_INSTR_PER_UNIT = {
-    "fp64": {"forces": 512.0, "nodes": 35.7, "kinematics": 368.0},
-    "mixed": {"forces": 8.0, "nodes": 27.0, "kinematics": 90.0},
+    "fp64": {"forces": 512.0, "nodes": 35.7, "kinematics": 368.0, "material": 205.3},
+    "mixed": {"forces": 8.0, "nodes": 27.0, "kinematics": 90.0, "material": 134.6},
 }
 # Double-precision operations per unit of the reference's formulation (adds,
 # multiplies, divides, square and cube roots each counted once), from
@@ -262,13 +261,13 @@ def roofline(prof: dict, precision: str, ne: int, nn: int, rep_avg: float,
         peak_rate = fp64_peak * 1e12 / 2  # DFMA thread instructions per second
         fp64_pipe = {"achieved_ginst_s": round(rate / 1e9, 1), "peak_ginst_s": round(peak_rate / 1e9, 1),
                      "frac": round(rate / peak_rate, 4), "instr_per_unit": ipu,
-                     "note": "FP64-pipe instructions per unit (ncu, s=100) x units / launch time; peak = "
+                     "note": "FP64-pipe instructions per unit (ncu, this workload) x units / launch time; peak = "
                              f"DFMA issue rate, {fp64_kind} (lulesh_probe_pipe_rates)"}
     return {
         "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
         "unit": "GB/s", "frac": sig4(achieved / peak),
         "traffic": tpu * units if tpu else None,
-        "traffic_note": "ncu dram bytes per unit at s=100 x units per launch" if tpu else None,
+        "traffic_note": "ncu dram bytes per unit on this workload x units per launch" if tpu else None,
         "peak_kind": f"{kind} ({'MEASURED_PEAKS.json hbm_gbs' if kind == 'measured' else 'recipe fallback'})",
         "bytes_per_launch": bytes_launch, "bytes_per_unit": BYTES_PER_UNIT[precision][dom],
         "avg_launch_ms": round(km[dom] / cyc, 4),

@@ -310,7 +310,7 @@ typedef struct lulesh_serve_stats {
     double wall_s;             /* start to the last finish */
     double device_s;           /* device time of the cycle replays */
     double zone_cycles_per_s;  /* all requests' zone-cycles / wall_s */
-    double p50_s, p99_s, mean_s; /* time to solution */
+    double p50_s, p99_s, mean_s; /* time to solution (quantiles interpolated between order statistics) */
     int64_t zone_cycles, launches;
     int32_t served, max_resident; /* requests served; most problems resident at once */
     int64_t peak_resident_bytes;  /* most pool bytes the resident problems held at once

@@ -22,12 +22,16 @@
 
 namespace {
 
-double quantile(std::vector<double> v, double q) {  // nearest rank
+// Quantile q of v with linear interpolation between order statistics (the
+// sample quantile of Hyndman and Fan's definition 7): for fewer than 100
+// samples p99 lies between the two largest instead of being the largest.
+double quantile(std::vector<double> v, double q) {
     if (v.empty()) return 0.0;
     std::sort(v.begin(), v.end());
-    size_t k = size_t(std::ceil(q * double(v.size())));
-    k = std::min(std::max<size_t>(k, 1), v.size());
-    return v[k - 1];
+    const double h = q * double(v.size() - 1);
+    const size_t lo = size_t(std::floor(h));
+    const size_t hi = std::min(lo + 1, v.size() - 1);
+    return v[lo] + (h - double(lo)) * (v[hi] - v[lo]);
 }
 
 }  // namespace

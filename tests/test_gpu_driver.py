@@ -43,7 +43,7 @@ def test_equals_form_and_ignored_flags(lulesh, golden_results):
     """--name=value as the reference's option parser takes it, and the
     reference's viz and HPX task-size flags accepted (no effect here)."""
     g = _golden(golden_results, 12, r=21)
-    out = subprocess.run([str(EXE), "--s=12", "--r=21", "--q", "--f", "2", "--v", "--elems-per-task=64",
+    out = subprocess.run([str(EXE), "--s=12", "--r=21", "--q", "--f", "2", "--elems-per-task=64",
                           "--task-size", "4", "--hpx:threads=2"],
                          capture_output=True, text=True, check=True).stdout.strip()
     s, r, cycles = out.split(",")[:3]

@@ -114,9 +114,10 @@ def test_roofline_arithmetic():
     assert fp["achieved_ginst_s"] == pytest.approx(rate / 1e9, rel=1e-3)
     assert fp["frac"] == pytest.approx(rate / 0.6e12, rel=1e-3)
     assert sum(rl["kernel_share"].values()) == pytest.approx(1.0, abs=1e-3)
-    # the material kernel has no fixed instruction count: no pipe roof claimed
+    # every kernel of both paths carries its measured FP64-pipe count
     prof["kernel_ms"]["material"] = 99.0
-    assert bench.roofline(prof, "fp64", ne, nn, 3.26)["fp64_pipe"] is None
+    rl = bench.roofline(prof, "mixed", ne, nn, 3.26)
+    assert rl["kernel"] == "material" and rl["fp64_pipe"]["instr_per_unit"] == 134.6
 
 
 def test_fom_matches_reference_report_formula():
