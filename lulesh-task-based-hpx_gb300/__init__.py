@@ -427,6 +427,8 @@ def probe_library() -> C.CDLL:
         lib.lulesh_probe_math.restype = C.c_int32
         lib.lulesh_probe_math.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                           C.c_int64]
+        lib.lulesh_probe_dmul.restype = C.c_int32
+        lib.lulesh_probe_dmul.argtypes = [C.POINTER(C.c_double)] * 4 + [C.c_int64]
         _probe_lib = lib
     return _probe_lib
 
@@ -453,6 +455,19 @@ def probe_math(fn: str, x):
                                        out.ctypes.data_as(C.POINTER(C.c_double)), xs.size),
            "lulesh_probe_math")
     return out
+
+
+def probe_dmul(a, b):
+    """The products a * b on the device by the FP64 pipe's multiply and by the
+    integer-pipe multiply the step kernels use; returns (native, ipipe)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    native, ipipe = np.empty_like(a), np.empty_like(a)
+    pd = C.POINTER(C.c_double)
+    _check(probe_library().lulesh_probe_dmul(a.ctypes.data_as(pd), b.ctypes.data_as(pd),
+                                             native.ctypes.data_as(pd), ipipe.ctypes.data_as(pd), a.size),
+           "lulesh_probe_dmul")
+    return native, ipipe
 
 
 def serve(requests: list[dict], precision: str = "mixed", hbm_budget: int = 160 << 30,

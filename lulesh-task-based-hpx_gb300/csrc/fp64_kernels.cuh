@@ -182,9 +182,9 @@ __device__ __forceinline__ void forces_from_geo(const Mesh& m, int i, const int 
         const double sc = rcp(determ) * (1.0 / 192.0);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            hx[k] = g.h[0][k] * sc;
-            hy[k] = g.h[1][k] * sc;
-            hz[k] = g.h[2][k] * sc;
+            hx[k] = pmul(g.h[0][k], sc);
+            hy[k] = pmul(g.h[1][k], sc);
+            hz[k] = pmul(g.h[2][k], sc);
         }
         hourgam_mode_h<0>(hg, hx[0], hy[0], hz[0], gx, gy, gz);
         hourgam_mode_h<1>(hg, hx[1], hy[1], hz[1], gx, gy, gz);
@@ -196,7 +196,7 @@ __device__ __forceinline__ void forces_from_geo(const Mesh& m, int i, const int 
 #pragma unroll
     for (int f = 0; f < 6; ++f)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) fa[f][d] = g.fa[f][d] * scale;
+        for (int d = 0; d < 3; ++d) fa[f][d] = pmul(g.fa[f][d], scale);
     const double coefficient = -m.prm.hgcoef * 0.01 * LD(m.ss + i) * LD(m.elemMass + i) * rcbrt_pos(determ);
     double* outs[3] = {m.fsx, m.fsy, m.fsz};
     const double* vels[3] = {m.xd, m.yd, m.zd};

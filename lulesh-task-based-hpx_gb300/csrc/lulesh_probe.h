@@ -28,6 +28,11 @@ int lulesh_probe_pipe_rates(double out[5]);
  * returned as doubles). n <= 2^26. */
 int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n);
 
+/* The double product of a[i] and b[i] for n pairs, by the FP64 pipe's
+ * multiply (native) and by the step's integer-pipe multiply (ipipe, which
+ * must give the same bits). n <= 2^26. */
+int lulesh_probe_dmul(const double* a, const double* b, double* native, double* ipipe, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

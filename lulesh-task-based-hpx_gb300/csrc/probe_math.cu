@@ -8,6 +8,7 @@
 #include "step_math.cuh"
 #include "float_pair.cuh"
 #include "lulesh_probe.h"
+#include "fp64_emu.cuh"
 
 namespace lulesh {
 namespace probe {
@@ -28,6 +29,17 @@ __global__ void k_math_probe(int fn, const double* __restrict__ in, double* __re
     else if (fn == 6) r = double(split(x).x);
     else r = double(split(x).y);
     out[i] = r;
+}
+
+__device__ __noinline__ double dmul_fp64_pipe(double a, double b) { return a * b; }
+
+// The FP64 pipe's product and the integer pipes' product of the same operands.
+__global__ void k_dmul_probe(const double* __restrict__ a, const double* __restrict__ b,
+                             double* __restrict__ native, double* __restrict__ ipipe, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    native[i] = dmul_fp64_pipe(a[i], b[i]);
+    ipipe[i] = dmul_ipipe(a[i], b[i]);
 }
 
 }  // namespace probe
@@ -53,5 +65,26 @@ extern "C" int lulesh_probe_math(int32_t fn, const double* in, double* out, int6
     }
     cudaFree(d_in);
     cudaFree(d_out);
+    return st;
+}
+
+extern "C" int lulesh_probe_dmul(const double* a, const double* b, double* native, double* ipipe, int64_t n) {
+    if (!a || !b || !native || !ipipe || n < 1 || n > (int64_t(1) << 26)) return LULESH_EINVAL;
+    const size_t bytes = sizeof(double) * size_t(n);
+    double* d = nullptr;
+    if (cudaMalloc(&d, 4 * bytes) != cudaSuccess) return LULESH_ENOMEM;
+    int st = LULESH_OK;
+    if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+        st = LULESH_ECUDA;
+    if (st == LULESH_OK) {
+        const int count = int(n);
+        lulesh::probe::k_dmul_probe<<<(count + 255) / 256, 256>>>(d, d + n, d + 2 * n, d + 3 * n, count);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(native, d + 2 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(ipipe, d + 3 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = LULESH_ECUDA;
+    }
+    cudaFree(d);
     return st;
 }

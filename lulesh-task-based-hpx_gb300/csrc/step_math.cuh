@@ -12,6 +12,7 @@
 // operation as the reference does.
 #pragma once
 
+#include "fp64_emu.cuh"
 #include "lulesh_dev.h"
 #include "portable_cbrt.h"
 
@@ -330,6 +331,14 @@ __device__ __forceinline__ double widen(float f) {
         (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
         (static_cast<unsigned long long>(e + 896u) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));
 }
+// A product for the FP64-bound kernels of the fast variants: double
+// multiplies run on the integer pipes (dmul_ipipe, the same bits as a * b),
+// beside the FP64 pipe's adds and multiply-adds; float ones stay plain.
+#if !LULESH_EXACT
+__device__ __forceinline__ double pmul(double a, double b) { return dmul_ipipe(a, b); }
+__device__ __forceinline__ float pmul(float a, float b) { return a * b; }
+#endif
+
 __device__ __forceinline__ double recip_sqrt(double b) { return rsqrt(b); }
 __device__ __forceinline__ float recip_sqrt(float b) { return rsqrtf(b); }
 
@@ -583,9 +592,9 @@ __device__ __forceinline__ void volume_gradient(const R J[3][3], const R c[3][3]
     R g[6][3];  // dV/dA_1..3, dV/dH_1..3, times 192
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        g[0][a] = R(3) * c[a][0];
-        g[1][a] = R(3) * c[a][1];
-        g[2][a] = R(3) * c[a][2];
+        g[0][a] = pmul(R(3), c[a][0]);
+        g[1][a] = pmul(R(3), c[a][1]);
+        g[2][a] = pmul(R(3), c[a][2]);
         g[3][a] = g[4][a] = g[5][a] = R(0);
     }
     cross_acc(H[2], H[1], g[0]);
@@ -700,10 +709,12 @@ __device__ __forceinline__ void fb_force_axis_plus(const R hg[8][4], const R vel
                                                    const R init[8], R out[8]) {
     R h[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m)
-        h[m] = (hg[0][m] * vel[0] + hg[1][m] * vel[1] + hg[2][m] * vel[2] + hg[3][m] * vel[3] +
-                hg[4][m] * vel[4] + hg[5][m] * vel[5] + hg[6][m] * vel[6] + hg[7][m] * vel[7]) *
-               coefficient;
+    for (int m = 0; m < 4; ++m) {
+        R d = pmul(hg[0][m], vel[0]);
+#pragma unroll
+        for (int k = 1; k < 8; ++k) d = fma(hg[k][m], vel[k], d);
+        h[m] = pmul(d, coefficient);
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         out[k] = init[k] + hg[k][0] * h[0] + hg[k][1] * h[1] + hg[k][2] * h[2] + hg[k][3] * h[3];

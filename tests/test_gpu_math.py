@@ -97,3 +97,42 @@ def test_split_is_the_float_pair(lulesh):
     want_lo = (x - want_hi).astype(np.float32).astype(np.float64)
     assert np.array_equal(hi, want_hi)
     assert np.array_equal(lo, want_lo)
+
+
+def test_integer_pipe_multiply_equals_fp64_pipe(lulesh):
+    """dmul_ipipe, the double multiply the fast kernels run on the integer
+    pipes, gives the FP64 pipe's bits for every operand pair: seeded random
+    bit patterns over the whole exponent range (normal, subnormal, zero,
+    infinite and NaN operands; products that overflow, underflow or land on
+    a rounding tie), plus products near powers of two and of small integers
+    (3 x c, the step's own pattern)."""
+    rng = np.random.default_rng(7)
+    n = 1 << 22
+    bits = rng.integers(0, 2 ** 63, size=(2, n), dtype=np.int64).astype(np.uint64)
+    bits[:, : n // 2] |= rng.integers(0, 2, size=(2, n // 2), dtype=np.uint64) << np.uint64(63)
+    a, b = bits.view(np.float64)
+    # operands in the step's range: exponents near 0, random significands
+    k = n // 4
+    a[:k] = np.ldexp(rng.uniform(1.0, 2.0, k), rng.integers(-60, 60, k)) * rng.choice([-1.0, 1.0], k)
+    b[:k] = np.ldexp(rng.uniform(1.0, 2.0, k), rng.integers(-60, 60, k))
+    b[k:k + 4096] = 3.0
+    b[k + 4096:k + 8192] = np.ldexp(1.0, rng.integers(-20, 20, 4096))
+    # significands whose product is (almost) a tie: a = 1 + 2^-26 j
+    a[2 * k:2 * k + 8192] = 1.0 + np.ldexp(rng.integers(1, 2 ** 26, 8192).astype(np.float64), -26)
+    b[2 * k:2 * k + 8192] = 1.0 + np.ldexp(rng.integers(1, 2 ** 26, 8192).astype(np.float64), -26)
+    # exponents that put the product at the edges of the normal range
+    e = rng.integers(-1000, 1000, 8192)
+    target = np.where(e > 0, 1024, -1074) + rng.integers(-8, 8, 8192)  # exponent of the product
+    a[3 * k:3 * k + 8192] = np.ldexp(rng.uniform(1.0, 2.0, 8192), e)
+    b[3 * k:3 * k + 8192] = np.ldexp(rng.uniform(1.0, 2.0, 8192), np.clip(target - e, -1074, 1023))
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -2.2e-308, 1e308, 1e-308, 1.0, -3.0])
+    sa, sb = np.meshgrid(special, special)
+    a[-sa.size:], b[-sb.size:] = sa.ravel(), sb.ravel()
+    native, ipipe = lulesh.probe_dmul(a, b)
+    same = native.view(np.uint64) == ipipe.view(np.uint64)
+    both_nan = np.isnan(native) & np.isnan(ipipe)
+    assert np.all(same | both_nan), np.flatnonzero(~(same | both_nan))[:8]
+    # and both are the IEEE products the host computes
+    with np.errstate(all="ignore"):
+        host = a * b
+    assert np.all((host.view(np.uint64) == native.view(np.uint64)) | (np.isnan(host) & np.isnan(native)))
