@@ -338,10 +338,10 @@ __device__ __forceinline__ void kinematics_elem(const Mesh& m, int i, double dt)
 // t x s: the reference's face measure is 4 |t x s|^2 (Lagrange's identity),
 // so the length is 2 V / sqrt(max |t x s|^2).
 __device__ __forceinline__ double char_length_faces(const double fa[6][3], double volume) {
-    double cl = fa[0][0] * fa[0][0] + fa[0][1] * fa[0][1] + fa[0][2] * fa[0][2];
+    double cl = fma(fa[0][2], fa[0][2], fma(fa[0][1], fa[0][1], pmul(fa[0][0], fa[0][0])));
 #pragma unroll
     for (int f = 1; f < 6; ++f)
-        cl = nonneg_max(cl, fa[f][0] * fa[f][0] + fa[f][1] * fa[f][1] + fa[f][2] * fa[f][2]);
+        cl = nonneg_max(cl, fma(fa[f][2], fa[f][2], fma(fa[f][1], fa[f][1], pmul(fa[f][0], fa[f][0]))));
     return div_sqrt(2.0 * volume, cl);
 }
 
@@ -372,7 +372,7 @@ __device__ __forceinline__ void kinematics_fast(const Mesh& m, int i, double dt)
     gather8(m.yd, nl, yv);
     gather8(m.zd, nl, zv);
     double gr[6];
-    m.vdov[i] = gradients_vdov_xc(g.J, g.c, xv, yv, zv, LD(m.volo + i) * relv, 0.5 * dt, gr);
+    m.vdov[i] = gradients_vdov_xc(g.J, g.c, xv, yv, zv, pmul(LD(m.volo + i), relv), 0.5 * dt, gr);
     m.dvxi[i] = gr[0];
     m.dveta[i] = gr[1];
     m.dvzeta[i] = gr[2];
@@ -437,7 +437,10 @@ __global__ void __launch_bounds__(kForceBlock) k_forces_geo(Mesh m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m.numElem) forces_geo_elem(m, i);
 }
-__global__ void __launch_bounds__(kKinBlock) k_kinematics_geo(Mesh m, double dt) {
+// At least 3 blocks of 128 per SM (at most 168 registers): with the
+// integer-pipe products the compiler's own choice, 240 registers and 2
+// blocks, left the FP64 pipe waiting (2.09 -> 2.00 ms at s=150).
+__global__ void __launch_bounds__(kKinBlock, 3) k_kinematics_geo(Mesh m, double dt) {
     if (m.dtime) {
         if (!m.dtime->active) return;
         dt = m.dtime->deltatime;
@@ -459,7 +462,10 @@ __global__ void __launch_bounds__(kForceBlock) k_geometry(Mesh m) {
 
 // Elements visited in repeat-count order so a warp's lanes run the same
 // number of EOS passes; the dt minima end in a last-block reduction.
-__global__ void __launch_bounds__(kMatBlock) k_material(Mesh m, int first, int end, int accumulate) {
+// 8 blocks of 128 per SM (64 registers): the EOS passes are a chain of
+// dependent integer-pipe products and FP64 operations, latency-bound at 6
+// blocks per SM (1.34 -> 1.02 ms at s=150 with 8).
+__global__ void __launch_bounds__(kMatBlock, 8) k_material(Mesh m, int first, int end, int accumulate) {
     if (m.dtime && !m.dtime->active) return;
     double dtc = 1.0e+20, dth = 1.0e+20;  // lulesh.cc:2214-2215
     for (int t = first + blockIdx.x * blockDim.x + threadIdx.x; t < end; t += gridDim.x * blockDim.x)

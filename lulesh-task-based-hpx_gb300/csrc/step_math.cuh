@@ -25,6 +25,18 @@ namespace LULESH_VARIANT {
 
 #define LD(p) __ldg(p)
 
+// A product for the FP64-bound kernels. Fast variants: double multiplies run
+// on the integer pipes (dmul_ipipe, the same bits as a * b), beside the FP64
+// pipe's adds and multiply-adds; a product written with pmul is never fused
+// into a multiply-add. Exact variant: the plain multiply, rounded on its own
+// as there every operation is. Float products stay plain.
+#if LULESH_EXACT
+__device__ __forceinline__ double pmul(double a, double b) { return a * b; }
+#else
+__device__ __forceinline__ double pmul(double a, double b) { return dmul_ipipe(a, b); }
+#endif
+__device__ __forceinline__ float pmul(float a, float b) { return a * b; }
+
 __device__ __forceinline__ void raise_error(StepResult* r, int elem, int phase) {
     if (atomicCAS(&r->err, 0, LULESH_EVOLUME) == 0) {
         r->err_elem = elem;
@@ -49,7 +61,13 @@ __device__ __forceinline__ void gather8(const double* __restrict__ f, const int 
 // TRIPLE_PRODUCT of lulesh.cc:649-651, arguments in the macro's order.
 template <class R>
 __device__ __forceinline__ R triple(R x1, R y1, R z1, R x2, R y2, R z2, R x3, R y3, R z3) {
+#if LULESH_EXACT
     return x1 * (y2 * z3 - z2 * y3) + x2 * (z1 * y3 - y1 * z3) + x3 * (y1 * z2 - z1 * y2);
+#else
+    // the first product of each pair and of the sum on the integer pipes
+    return fma(x3, fma(-z1, y2, pmul(y1, z2)),
+               fma(x2, fma(-y1, z3, pmul(z1, y3)), pmul(x1, fma(-z2, y3, pmul(y2, z3)))));
+#endif
 }
 
 // CalcElemVolume (lulesh.cc:592-665).
@@ -71,8 +89,7 @@ __device__ __forceinline__ R hex_volume(const R x[8], const R y[8], const R z[8]
     R vol = triple(dx31 + dx72, dx63, dx20, dy31 + dy72, dy63, dy20, dz31 + dz72, dz63, dz20) +
             triple(dx43 + dx57, dx64, dx70, dy43 + dy57, dy64, dy70, dz43 + dz57, dz64, dz70) +
             triple(dx14 + dx25, dx61, dx50, dy14 + dy25, dy61, dy50, dz14 + dz25, dz61, dz50);
-    vol *= twelveth;
-    return vol;
+    return pmul(vol, twelveth);
 }
 
 // Centre Jacobian of CalcElemShapeFunctionDerivatives (lulesh.cc:277-305).
@@ -124,15 +141,16 @@ __device__ __forceinline__ void dirs(const R v[8], R d[3]) {
 // c[0][0] is the reference's cjxxi, c[0][1] its cjxet, ...).
 template <class R>
 __device__ __forceinline__ void cofactors(const R J[3][3], R c[3][3]) {
-    c[0][0] = J[1][1] * J[2][2] - J[2][1] * J[1][2];
-    c[0][1] = J[2][0] * J[1][2] - J[1][0] * J[2][2];
-    c[0][2] = J[1][0] * J[2][1] - J[2][0] * J[1][1];
-    c[1][0] = J[2][1] * J[0][2] - J[0][1] * J[2][2];
-    c[1][1] = J[0][0] * J[2][2] - J[2][0] * J[0][2];
-    c[1][2] = J[2][0] * J[0][1] - J[0][0] * J[2][1];
-    c[2][0] = J[0][1] * J[1][2] - J[1][1] * J[0][2];
-    c[2][1] = J[1][0] * J[0][2] - J[0][0] * J[1][2];
-    c[2][2] = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+    // a * b - c * d as fma(-c, d, a * b), the first product on the integer pipes
+    c[0][0] = fma(-J[2][1], J[1][2], pmul(J[1][1], J[2][2]));
+    c[0][1] = fma(-J[1][0], J[2][2], pmul(J[2][0], J[1][2]));
+    c[0][2] = fma(-J[2][0], J[1][1], pmul(J[1][0], J[2][1]));
+    c[1][0] = fma(-J[0][1], J[2][2], pmul(J[2][1], J[0][2]));
+    c[1][1] = fma(-J[2][0], J[0][2], pmul(J[0][0], J[2][2]));
+    c[1][2] = fma(-J[0][0], J[2][1], pmul(J[2][0], J[0][1]));
+    c[2][0] = fma(-J[1][1], J[0][2], pmul(J[0][1], J[1][2]));
+    c[2][1] = fma(-J[0][0], J[1][2], pmul(J[1][0], J[0][2]));
+    c[2][2] = fma(-J[1][0], J[0][1], pmul(J[0][0], J[1][1]));
 }
 #endif
 
@@ -224,7 +242,7 @@ __device__ __forceinline__ R quot(R a, R b) {
 #if LULESH_EXACT
     return a / b;
 #else
-    return a * rcp(b);
+    return pmul(a, rcp(b));
 #endif
 }
 
@@ -238,7 +256,7 @@ __device__ __forceinline__ double quot_refined(double a, double b) {
     return a / b;
 #else
     const double y = rcp(b);
-    const double q = a * y;
+    const double q = pmul(a, y);
     return fma(fma(-b, q, a), y, q);
 #endif
 }
@@ -331,14 +349,6 @@ __device__ __forceinline__ double widen(float f) {
         (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
         (static_cast<unsigned long long>(e + 896u) << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29)));
 }
-// A product for the FP64-bound kernels of the fast variants: double
-// multiplies run on the integer pipes (dmul_ipipe, the same bits as a * b),
-// beside the FP64 pipe's adds and multiply-adds; float ones stay plain.
-#if !LULESH_EXACT
-__device__ __forceinline__ double pmul(double a, double b) { return dmul_ipipe(a, b); }
-__device__ __forceinline__ float pmul(float a, float b) { return a * b; }
-#endif
-
 __device__ __forceinline__ double recip_sqrt(double b) { return rsqrt(b); }
 __device__ __forceinline__ float recip_sqrt(float b) { return rsqrtf(b); }
 
@@ -362,7 +372,7 @@ __device__ __forceinline__ double rcbrt_pos(double x) {
 // Square root of a positive normal double in the fast variants: x times the
 // library's reciprocal square root, one rounding more than sqrt (within
 // about one ulp; the probe test measures it) for fewer FP64-pipe slots.
-__device__ __forceinline__ double sqrt_fast(double x) { return x * rsqrt(x); }
+__device__ __forceinline__ double sqrt_fast(double x) { return pmul(x, rsqrt(x)); }
 #endif
 
 template <class R>
@@ -370,7 +380,7 @@ __device__ __forceinline__ R div_sqrt(R a, R b) {
 #if LULESH_EXACT
     return a / sqrt(b);
 #else
-    return a * recip_sqrt(b);
+    return pmul(a, recip_sqrt(b));
 #endif
 }
 
@@ -408,9 +418,9 @@ template <int A, int B, int C, int D, class R>
 __device__ __forceinline__ void face_txs(const R x[8], const R y[8], const R z[8], R a[3]) {
     const R sx = x[C] - x[A], sy = y[C] - y[A], sz = z[C] - z[A];
     const R tx = x[D] - x[B], ty = y[D] - y[B], tz = z[D] - z[B];
-    a[0] = ty * sz - tz * sy;
-    a[1] = tz * sx - tx * sz;
-    a[2] = tx * sy - ty * sx;
+    a[0] = fma(-tz, sy, pmul(ty, sz));
+    a[1] = fma(-tx, sz, pmul(tz, sx));
+    a[2] = fma(-ty, sx, pmul(tx, sy));
 }
 #endif
 
@@ -885,12 +895,12 @@ __device__ __forceinline__ R gradients_vdov_xc(const R X[3][3], const R cx[3][3]
 #pragma unroll
         for (int d = 0; d < 3; ++d) c[a][d] = cx[a][d];
     const R pt = R(256.0) * R(1.e-36);
-    const R vol16 = R(16.0) * vol;
-    const R n64 = rcp(vol + R(1.e-36)) * R(0.015625);
+    const R vol16 = pmul(R(16.0), vol);
+    const R n64 = pmul(rcp(vol + R(1.e-36)), R(0.015625));
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        g[3 + d] = vol16 * recip_sqrt(c[0][d] * c[0][d] + c[1][d] * c[1][d] + c[2][d] * c[2][d] + pt);
-        g[d] = (c[0][d] * V[0][d] + c[1][d] * V[1][d] + c[2][d] * V[2][d]) * n64;
+        g[3 + d] = pmul(vol16, recip_sqrt(fma(c[2][d], c[2][d], fma(c[1][d], c[1][d], pmul(c[0][d], c[0][d]))) + pt));
+        g[d] = pmul(fma(c[2][d], V[2][d], fma(c[1][d], V[1][d], pmul(c[0][d], V[0][d]))), n64);
     }
     R J[3][3];
 #pragma unroll
@@ -898,8 +908,8 @@ __device__ __forceinline__ R gradients_vdov_xc(const R X[3][3], const R cx[3][3]
 #pragma unroll
         for (int d = 0; d < 3; ++d) J[a][d] = X[a][d] - dt2 * V[a][d];
     cofactors(J, c);
-    const R det = J[0][0] * c[0][0] + J[0][1] * c[0][1] + J[0][2] * c[0][2];
-    R num = c[0][0] * V[0][0];
+    const R det = fma(J[0][2], c[0][2], fma(J[0][1], c[0][1], pmul(J[0][0], c[0][0])));
+    R num = pmul(c[0][0], V[0][0]);
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -963,11 +973,11 @@ __device__ __forceinline__ R limiter(const R* __restrict__ dv, int i, int bm, in
     if (bp == comm_p || bp == 0) delvp = LD(dv + np);
     else if (bp == symm_p) delvp = self;
     else delvp = R(0.0);
-    delvm = delvm * norm;
-    delvp = delvp * norm;
-    R phi = R(.5) * (delvm + delvp);
-    delvm *= mult;
-    delvp *= mult;
+    delvm = pmul(delvm, norm);
+    delvp = pmul(delvp, norm);
+    R phi = pmul(R(.5), delvm + delvp);
+    delvm = pmul(delvm, mult);
+    delvp = pmul(delvp, mult);
     if (f_vlt(delvm, phi)) phi = delvm;
     if (f_vlt(delvp, phi)) phi = delvp;
     if (f_lt(phi, R(0.))) phi = R(0.);
@@ -997,18 +1007,19 @@ __device__ __forceinline__ void q_terms(const Mesh& m, int i, const R* dvxi, con
         qq = 0.;
         return;
     }
-    R dxi = LD(dvxi + i) * LD(dxxi + i);
-    R deta = LD(dveta + i) * LD(dxeta + i);
-    R dzeta = LD(dvzeta + i) * LD(dxzeta + i);
+    R dxi = pmul(LD(dvxi + i), LD(dxxi + i));
+    R deta = pmul(LD(dveta + i), LD(dxeta + i));
+    R dzeta = pmul(LD(dvzeta + i), LD(dxzeta + i));
     if (f_gt(dxi, R(0.))) dxi = R(0.);
     if (f_gt(deta, R(0.))) deta = R(0.);
     if (f_gt(dzeta, R(0.))) dzeta = R(0.);
-    const R rho = R(quot(LD(m.elemMass + i), LD(m.volo + i) * vnew));
-    const R qlin = -R(P.qlc_monoq) * rho *
-                   (dxi * (R(1.) - phixi) + deta * (R(1.) - phieta) + dzeta * (R(1.) - phizeta));
-    const R qquad = R(P.qqc_monoq) * rho *
-                    (dxi * dxi * (R(1.) - phixi * phixi) + deta * deta * (R(1.) - phieta * phieta) +
-                     dzeta * dzeta * (R(1.) - phizeta * phizeta));
+    const R rho = R(quot(LD(m.elemMass + i), pmul(LD(m.volo + i), vnew)));
+    const R qlin = pmul(pmul(-R(P.qlc_monoq), rho),
+                        pmul(dxi, R(1.) - phixi) + pmul(deta, R(1.) - phieta) + pmul(dzeta, R(1.) - phizeta));
+    const R qquad = pmul(pmul(R(P.qqc_monoq), rho),
+                         pmul(pmul(dxi, dxi), R(1.) - pmul(phixi, phixi)) +
+                         pmul(pmul(deta, deta), R(1.) - pmul(phieta, phieta)) +
+                         pmul(pmul(dzeta, dzeta), R(1.) - pmul(phizeta, phizeta)));
     ql = double(qlin);
     qq = double(qquad);
 }
@@ -1141,7 +1152,7 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
 // the full-step term 2/3 vnewc^2 p. The repeat loop stays real work as in
 // the exact variant.
 __device__ __forceinline__ double pressure(double bvc, double e, double vnewc, const lulesh_params& P) {
-    double nv = bvc * e;
+    double nv = pmul(bvc, e);
     if (f_abs_lt(nv, P.p_cut) || f_ge(vnewc, P.eosvmax)) nv = 0.0;
     if (f_lt(nv, P.pmin)) nv = P.pmin;
     return nv;
@@ -1160,7 +1171,7 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
         double p_old = m.p[i];
         const double qq_old = m.qq[i], ql_old = m.ql[i];
         const double vchalf = vnewc - delvc * .5;
-        double bvcf = cls * rcp(vnewc), bvch = cls * rcp(vchalf);
+        double bvcf = pmul(cls, rcp(vnewc)), bvch = pmul(cls, rcp(vchalf));
         double vh = vchalf;
         vf = vnewc;
         if (vmin_on && f_le(vnewc, P.eosvmin)) {
@@ -1174,31 +1185,32 @@ __device__ __forceinline__ double eos_body(const Mesh& m, int i, double vnewc, i
             vf = vnewc * vnewc;
         }
         const double pq_old = p_old + q_old;
+        const double hdelv = pmul(0.5, delvc);
         // predictor
-        e_new = e_old - 0.5 * delvc * pq_old;
+        e_new = fma(-hdelv, pq_old, e_old);
         if (f_lt(e_new, P.emin)) e_new = P.emin;
         const double pHalf = pressure(bvch, e_new, vnewc, P);
         if (f_gt(delvc, 0.)) q_new = 0.;
-        else q_new = q_sound(over_rho<UNIT_RHO>(cls * (e_new + vh * pHalf), P)) * ql_old + qq_old;
+        else q_new = fma(q_sound(over_rho<UNIT_RHO>(pmul(cls, fma(vh, pHalf, e_new)), P)), ql_old, qq_old);
         const double pq_half = pHalf + q_new;
-        e_new = e_new + 0.5 * delvc * (3.0 * pq_old - 4.0 * pq_half);
+        e_new = fma(hdelv, fma(-4.0, pq_half, pmul(3.0, pq_old)), e_new);
         if (f_abs_lt(e_new, P.e_cut)) e_new = 0.0;
         if (f_lt(e_new, P.emin)) e_new = P.emin;
         p_new = pressure(bvcf, e_new, vnewc, P);
         // corrector
         double q_tilde;
         if (f_gt(delvc, 0.)) q_tilde = 0.;
-        else q_tilde = q_sound(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
-        e_new = e_new - (7.0 * pq_old - 8.0 * pq_half + (p_new + q_tilde)) * (delvc * (1.0 / 6.0));
+        else q_tilde = fma(q_sound(over_rho<UNIT_RHO>(pmul(cls, fma(vf, p_new, e_new)), P)), ql_old, qq_old);
+        e_new = fma(-(fma(-8.0, pq_half, pmul(7.0, pq_old)) + (p_new + q_tilde)), pmul(delvc, 1.0 / 6.0), e_new);
         if (f_abs_lt(e_new, P.e_cut)) e_new = 0.;
         if (f_lt(e_new, P.emin)) e_new = P.emin;
         p_new = pressure(bvcf, e_new, vnewc, P);
         if (f_le(delvc, 0.)) {
-            q_new = q_sound(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P)) * ql_old + qq_old;
+            q_new = fma(q_sound(over_rho<UNIT_RHO>(pmul(cls, fma(vf, p_new, e_new)), P)), ql_old, qq_old);
             if (f_abs_lt(q_new, P.q_cut)) q_new = 0.;
         }
     }
-    const double sst = ss_guard(over_rho<UNIT_RHO>(cls * (e_new + vf * p_new), P));
+    const double sst = ss_guard(over_rho<UNIT_RHO>(pmul(cls, fma(vf, p_new, e_new)), P));
     m.ss[i] = sst;
     m.p[i] = p_new;
     m.e[i] = e_new;
@@ -1217,8 +1229,13 @@ __device__ __forceinline__ bool dt_candidates(const lulesh_params& P, double ss,
                                               double arealg, double& courant, double& hydro) {
     if (f_is_zero(vdov)) return false;
     const double qqc2 = 64.0 * P.qqc * P.qqc;
+#if LULESH_EXACT
     double dtf = ss * ss;
     if (f_lt(vdov, 0.0)) dtf += qqc2 * arealg * arealg * vdov * vdov;
+#else
+    double dtf = pmul(ss, ss);
+    if (f_lt(vdov, 0.0)) dtf = fma(pmul(qqc2, pmul(arealg, arealg)), pmul(vdov, vdov), dtf);
+#endif
     courant = div_sqrt(arealg, dtf);  // arealg / sqrt(dtf)
     hydro = quot(P.dvovmax, fabs(vdov) + 1.e-20);
     return true;
@@ -1307,7 +1324,7 @@ __device__ __forceinline__ void node_update(const Mesh& m, int n, double fx, dou
 #else
     // fast variants: the reciprocal nodal mass is precomputed once per handle
     const double im = LD(m.invMass + n);
-    double ax = fx * im, ay = fy * im, az = fz * im;
+    double ax = pmul(fx, im), ay = pmul(fy, im), az = pmul(fz, im);
 #endif
     const unsigned sym = LD(m.nodeSymm + n);
     if (sym & 1u) ax = 0.0;
