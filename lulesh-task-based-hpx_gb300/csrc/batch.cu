@@ -93,6 +93,7 @@ struct Slot {
     int s = 0, numElem = 0, numNode = 0;
     std::vector<int32_t> repCount;  // elements per EOS repeat class, classes in matOrder order
     std::vector<int32_t> repValue;
+    bool finished = false;  // reached its stoptime, cycle limit or an error (seen by lulesh_batch_run)
 };
 
 struct Launch3 {
@@ -233,14 +234,32 @@ BatchLaunch shape(const lulesh_batch* b, int phase) {
     return {block, b->sms * per_sm, std::max(1, b->tuning.grab[phase])};
 }
 
-// Rebuilds the three tile tables from the slots in use. Returns true when a
-// table outgrew its device capacity (the caller reallocates and re-captures).
+// Tile size for the problems still running: the tuned size, halved (down to
+// 64) while the running problems' elements would give each resident block
+// of the widest phase fewer than 4 tiles. When the first problems of an
+// ensemble finish, the rest then still spread over every SM instead of a few
+// long tiles.
+int effective_tile(const lulesh_batch* b) {
+    int64_t elems = 0;
+    for (const Slot& sl : b->slots)
+        if (sl.in_use && !sl.finished) elems += sl.numElem;
+    int blocks = 1;
+    for (int p = 0; p < 4; ++p) blocks = std::max(blocks, shape(b, p).grid);
+    int T = std::max(32, b->tuning.tile);
+    while (T > 64 && elems < int64_t(4) * blocks * T) T /= 2;
+    return T;
+}
+
+// Rebuilds the three tile tables from the slots in use, leaving out problems
+// already finished (their tiles would only be fetched and skipped). Returns
+// true when a table outgrew its device capacity (the caller reallocates and
+// re-captures).
 bool rebuild_tiles(lulesh_batch* b) {
-    const int T = std::max(32, b->tuning.tile);
+    const int T = effective_tile(b);
     for (auto& t : b->h_tiles) t.clear();
     for (int s = 0; s < int(b->slots.size()); ++s) {
         const Slot& sl = b->slots[s];
-        if (!sl.in_use) continue;
+        if (!sl.in_use || sl.finished) continue;
         for (int e = 0; e < sl.numElem; e += T)
             b->h_tiles[lulesh::TILES_ELEM].push_back({s, e, std::min(T, sl.numElem - e), std::min(T, sl.numElem - e)});
         for (int n = 0; n < sl.numNode; n += T)
@@ -539,6 +558,14 @@ int lulesh_batch_run(lulesh_batch* b, int32_t cycles, int32_t* active_slots, dou
     if (st != LULESH_OK) return st;
     st = refresh_status(b);
     if (st != LULESH_OK) return st;
+    // problems that finished in these cycles leave the tile tables
+    for (size_t i = 0; i < b->slots.size(); ++i) {
+        Slot& sl = b->slots[i];
+        if (sl.in_use && !sl.finished && !b->h_times[i].active) {
+            sl.finished = true;
+            b->tiles_dirty = true;
+        }
+    }
     if (active_slots) {
         int n = 0;
         for (size_t i = 0; i < b->slots.size(); ++i) n += (b->slots[i].in_use && b->h_times[i].active);
