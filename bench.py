@@ -83,16 +83,18 @@ LAYOUT_BYTES_PER_UNIT = {
 }
 # DRAM bytes (read + write) and FP64-pipe instructions (thread level:
 # sm__inst_executed_pipe_fp64 x 32) per unit, measured by ncu on this
-# workload (s=150 r=21, the second and third cycles); every array a kernel
-# streams is larger than L2. The material kernel's count depends on the
-# state (EOS passes, compressing elements); these are early cycles of the run.
+# workload (s=150 r=21, the third cycle); every array a kernel streams is
+# larger than L2. The material kernel's count depends on the state (EOS
+# passes, compressing elements); these are early cycles of the run. The FP64
+# pipe carries only part of the double arithmetic: the fast kernels run many
+# of their multiplies on the integer pipes (dmul_ipipe).
 TRAFFIC_PER_UNIT = {
-    "fp64": {"forces": 672, "nodes": 368, "kinematics": 550, "material": 227},
-    "mixed": {"forces": 215, "nodes": 314, "kinematics": 177, "material": 198},
+    "fp64": {"forces": 672, "nodes": 368, "kinematics": 563, "material": 230},
+    "mixed": {"forces": 215, "nodes": 315, "kinematics": 178, "material": 199},
 }
 FP64_INSTR_PER_UNIT = {
-    "fp64": {"forces": 512.0, "nodes": 35.7, "kinematics": 368.0, "material": 205.3},
-    "mixed": {"forces": 8.0, "nodes": 27.0, "kinematics": 90.0, "material": 134.6},
+    "fp64": {"forces": 449.0, "nodes": 32.7, "kinematics": 320.0, "material": 136.1},
+    "mixed": {"forces": 8.0, "nodes": 24.0, "kinematics": 76.0, "material": 115.1},
 }
 # Double-precision operations per unit of the reference's formulation (adds,
 # multiplies, divides, square and cube roots each counted once), from

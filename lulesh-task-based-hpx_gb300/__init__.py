@@ -434,10 +434,12 @@ def probe_library() -> C.CDLL:
 
 
 def pipe_rates() -> dict:
-    """Measured double FMA/add/divide/sqrt and float FMA rates (ops/s) of the current GPU."""
-    out = (C.c_double * 5)()
+    """Measured rates (ops/s) of the current GPU: double FMA, add, divide, sqrt,
+    float FMA, and double multiplies on the FP64 pipe, on the integer pipes
+    (dmul_ipipe) and on both at once."""
+    out = (C.c_double * 8)()
     _check(probe_library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
-    return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma"), list(out)))
+    return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma", "dmul", "dmul_ipipe", "dmul_both"), list(out)))
 
 
 MATH_FUNCTIONS = {"rcp": 0, "rcbrt": 1, "sqrt": 2, "rsqrt": 3, "rcp_seed": 4, "narrow": 5, "split_hi": 6,

@@ -15,9 +15,11 @@ extern "C" {
 
 /* Measures the current GPU's pipe rates: out[0] double FMA/s, out[1] double
  * add/s, out[2] double divide/s, out[3] double square root/s, out[4] float
- * FMA/s (per-thread operations). The double path is bound by out[0]; takes
- * about 50 ms. Returns 0 or a LULESH_* status. */
-int lulesh_probe_pipe_rates(double out[5]);
+ * FMA/s, out[5] double multiplies/s on the FP64 pipe, out[6] the same on the
+ * integer pipes (the step's dmul_ipipe), out[7] both at once (half of the
+ * chains each); per-thread operations. The double path is bound by out[0];
+ * takes about 60 ms. Returns 0 or a LULESH_* status. */
+int lulesh_probe_pipe_rates(double out[8]);
 
 /* Evaluates one arithmetic helper of the fast variants on the device for n
  * inputs (accuracy tests compare the results with correctly rounded host

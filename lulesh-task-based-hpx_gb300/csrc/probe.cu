@@ -10,6 +10,7 @@
 
 #include "lulesh_gb300.h"
 #include "lulesh_probe.h"
+#include "fp64_emu.cuh"
 
 namespace {
 
@@ -25,6 +26,9 @@ __global__ void k_probe(double* out, int iters, double a, double b) {
             if (OP == 1) r[k] = r[k] + b;
             if (OP == 2) r[k] = a / r[k];
             if (OP == 3) r[k] = sqrt(r[k] + b);
+            if (OP == 4) r[k] = r[k] * a;                                   // FP64 pipe multiply
+            if (OP == 5) r[k] = lulesh::dmul_ipipe(r[k], a);                // integer-pipe multiply
+            if (OP == 6) r[k] = (k & 1) ? lulesh::dmul_ipipe(r[k], a) : r[k] * a;  // half each
         }
     }
     double s = 0.0;
@@ -48,7 +52,7 @@ __global__ void k_probe_f32(float* out, int iters, float a, float b) {
 
 }  // namespace
 
-extern "C" int lulesh_probe_pipe_rates(double out[5]) {
+extern "C" int lulesh_probe_pipe_rates(double out[8]) {
     if (!out) return LULESH_EINVAL;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return LULESH_ENODEV;
@@ -60,9 +64,9 @@ extern "C" int lulesh_probe_pipe_rates(double out[5]) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int iters[5] = {2000, 2000, 200, 200, 20000};
+    const int iters[8] = {2000, 2000, 200, 200, 20000, 2000, 2000, 2000};
     int st = LULESH_OK;
-    for (int op = 0; op < 5 && st == LULESH_OK; ++op) {
+    for (int op = 0; op < 8 && st == LULESH_OK; ++op) {
         float ms = 0.f;
         for (int rep = 0; rep < 2; ++rep) {  // first pass warms up
             cudaEventRecord(e0);
@@ -72,7 +76,10 @@ extern "C" int lulesh_probe_pipe_rates(double out[5]) {
                 case 1: k_probe<1><<<blocks, threads>>>(d, iters[op], 0.999999, 1e-6); break;
                 case 2: k_probe<2><<<blocks, threads>>>(d, iters[op], 1.000001, 1e-6); break;
                 case 3: k_probe<3><<<blocks, threads>>>(d, iters[op], 1.000001, 1e-6); break;
-                default: k_probe_f32<<<blocks, threads>>>(static_cast<float*>(buf), iters[op], 0.999999f, 1e-6f);
+                case 4: k_probe_f32<<<blocks, threads>>>(static_cast<float*>(buf), iters[op], 0.999999f, 1e-6f); break;
+                case 5: k_probe<4><<<blocks, threads>>>(d, iters[op], 0.999999, 0.0); break;
+                case 6: k_probe<5><<<blocks, threads>>>(d, iters[op], 0.999999, 0.0); break;
+                default: k_probe<6><<<blocks, threads>>>(d, iters[op], 0.999999, 0.0);
             }
             cudaEventRecord(e1);
             if (cudaEventSynchronize(e1) != cudaSuccess) st = LULESH_ECUDA;

@@ -117,7 +117,7 @@ def test_roofline_arithmetic():
     # every kernel of both paths carries its measured FP64-pipe count
     prof["kernel_ms"]["material"] = 99.0
     rl = bench.roofline(prof, "mixed", ne, nn, 3.26)
-    assert rl["kernel"] == "material" and rl["fp64_pipe"]["instr_per_unit"] == 134.6
+    assert rl["kernel"] == "material" and rl["fp64_pipe"]["instr_per_unit"] == bench.FP64_INSTR_PER_UNIT["mixed"]["material"]
 
 
 def test_fom_matches_reference_report_formula():
