@@ -32,9 +32,11 @@ ours (default) prints one JSON line:
   cpu_baseline   the CPU oracle (a bit-exact restatement of the reference's
                  code) on this machine's host cores, bounded sample (the
                  reference's reduced s=150 cap of 180 cycles); its sweep
-                 adds the single-thread rate
+                 adds the single-thread rate, and reference_code_1_thread
+                 the reference's own sources built on this host (sequential
+                 HPX stand-in) where they are installed
 reference: the reference's CPU algorithm (the oracle port) on all host cores,
-same workload, same metric.
+same workload, same metric (plus reference_code_1_thread).
 
 Multi-GPU: the step does not shard inside one problem (replicas only); with
 N ranks every rank runs its own s=150 problem and value sums them (weak
@@ -325,6 +327,32 @@ def cpu_oracle_rate(s: int, r: int, cycles: int, threads: int) -> tuple[float, f
     return ne * cycles / dt, dt
 
 
+def reference_code_rate(s: int, r: int, cycles: int) -> dict | None:
+    """The reference's own code on this host: its unmodified lulesh.cc,
+    lulesh-init.cc and lulesh-viz.cc built here against the sequential HPX
+    stand-in (oracle/_ref/lulesh-ref, from the checkout or its installed copy
+    in baseline/_ref), so one thread. Rate = elements x cycles / the elapsed
+    time the reference itself measures around its time loop
+    (lulesh.cc:2388-2392). None where the sources are not on this machine."""
+    import oracle
+
+    if not oracle.REF_BIN.exists():
+        if not (oracle.REF_SOURCES / "lulesh.cc").exists():
+            return None
+        oracle.build(ref=True)
+    r_ = subprocess.run([str(oracle.REF_BIN), "--s", str(s), "--r", str(r), "--i", str(cycles)],
+                        capture_output=True, text=True, timeout=600)
+    line = next((x for x in r_.stdout.splitlines() if x.startswith("RESULT ")), None)
+    if r_.returncode != 0 or line is None:
+        return None
+    kv = dict(x.split("=", 1) for x in line.split()[1:])
+    elapsed = float(kv["elapsed"])
+    return {"value": round(s ** 3 * cycles / elapsed, 1), "unit": UNIT, "threads": 1,
+            "sample": f"{cycles} cycles of s={s} r={r} ({elapsed:.1f} s by the reference's own timer)",
+            "code": "the reference's unmodified sources with the sequential HPX stand-in, built on this "
+                    "host (-O3 -ffp-contract=off)"}
+
+
 def run_ours(args) -> None:
     rank, world, local = dist_init()
     lul = load_package()
@@ -429,6 +457,11 @@ def run_ours(args) -> None:
             cpu["sweep"] = {"threads": [1, threads], "value": [round(rate1, 1), round(rate, 1)],
                             "sample_1_thread": f"{args.cpu_cycles_1t} cycles of s={s} r={r} after 1 "
                                                f"warm-up cycle ({secs1:.1f} s)"}
+            # the reference's own code at one thread, beside the port's
+            refc = reference_code_rate(s, r, args.cpu_cycles_1t)
+            if refc:
+                refc["port_1_thread_over_reference"] = round(rate1 / refc["value"], 3)
+                cpu["reference_code_1_thread"] = refc
 
     if rank != 0:
         return
@@ -612,11 +645,15 @@ def run_reference(args) -> None:
                    "elements": ne},
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{K} cycles of s={s} r={r} after {W} warm-up cycles; the "
-                                   "reference's algorithm as the bit-exact C oracle (the reference "
-                                   "sources and HPX are not on this machine), OpenMP over all "
-                                   "host threads"},
+                                   "reference's algorithm as the bit-exact C oracle, OpenMP over all "
+                                   "host threads (HPX is not installed, so the reference's own code "
+                                   "runs here only sequentially: reference_code_1_thread)"},
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if args.cpu_cycles_1t > 0:
+        refc = reference_code_rate(s, r, args.cpu_cycles_1t)
+        if refc:
+            out["cpu_baseline"]["reference_code_1_thread"] = refc
     print(json.dumps(out), flush=True)
 
 

@@ -36,13 +36,23 @@ NODE_FIELDS = ("x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy",
 ELEM_FIELDS = ("e", "p", "q", "ql", "qq", "v", "vnew", "delv", "vdov", "arealg", "ss")
 
 
+# The installed copy of the reference (oracle/Makefile install-ref): its
+# unmodified sources, for machines without the checkout.
+REF_INSTALLED = HERE.parent / "baseline" / "_ref"
+
+
 def build(ref: bool | None = None) -> None:
-    """Builds the port (always) and the reference binary (when its sources exist)."""
+    """Builds the port (always) and the reference binary (when its sources
+    exist). Where the checkout exists, its sources are also installed into
+    baseline/_ref, so that a machine without it (the GPU host) can build and
+    time the reference's own code."""
     subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
     if ref is None:
         ref = REF_SOURCES.is_dir()
     if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_DIR={REF_SOURCES}"], check=True)
+        subprocess.run(["make", "-s", "-j2", "-C", str(HERE), "ref", f"REF_DIR={REF_SOURCES}"], check=True)
+        if REF_SOURCES.resolve() != REF_INSTALLED.resolve():
+            subprocess.run(["make", "-s", "-C", str(HERE), "install-ref"], check=True)
 
 
 _lib = None
