@@ -29,6 +29,9 @@ struct Launchers {
     int (*forces_geo)(const Mesh&, cudaStream_t);
     int (*kinematics_geo)(const Mesh&, double, cudaStream_t);
     int (*geometry)(const Mesh&, cudaStream_t);
+    // lulesh_leapfrog's kinematics slabs: elements [first, end)
+    int (*kinematics_range)(const Mesh&, double, int, int, cudaStream_t);
+    int (*kinematics_geo_range)(const Mesh&, double, int, int, cudaStream_t);
 };
 
 Launchers launchers_for(int precision) {
@@ -38,17 +41,17 @@ Launchers launchers_for(int precision) {
                     lulesh::fp64::launch_kinematics, lulesh::fp64::launch_material,
                     lulesh::fp64::launch_forces_range, lulesh::fp64::launch_material_range,
                     lulesh::fp64::launch_forces_geo, lulesh::fp64::launch_kinematics_geo,
-                    lulesh::fp64::launch_geometry};
+                    lulesh::fp64::launch_geometry, lulesh::fp64::launch_kinematics_range, lulesh::fp64::launch_kinematics_geo_range};
         case LULESH_FP64_EXACT:
             return {lulesh::fp64x::launch_forces, lulesh::fp64x::launch_nodes,
                     lulesh::fp64x::launch_kinematics, lulesh::fp64x::launch_material,
                     lulesh::fp64x::launch_forces_range, lulesh::fp64x::launch_material_range,
-                    nullptr, nullptr, nullptr};
+                    nullptr, nullptr, nullptr, lulesh::fp64x::launch_kinematics_range, nullptr};
         default:
             return {lulesh::mixed::launch_forces, lulesh::mixed::launch_nodes,
                     lulesh::mixed::launch_kinematics, lulesh::mixed::launch_material,
                     lulesh::mixed::launch_forces_range, lulesh::mixed::launch_material_range,
-                    nullptr, nullptr, nullptr};
+                    nullptr, nullptr, nullptr, lulesh::mixed::launch_kinematics_range, nullptr};
     }
 }
 
@@ -73,7 +76,7 @@ struct lulesh_dev {
     void* arena = nullptr;
     size_t arena_bytes = 0;
     Mesh m{};
-    StepResult* h_result = nullptr;  // pinned
+    StepResult* h_result = nullptr;  // pinned: [0] the step's, [1 + k] material slab k's (lulesh_leapfrog)
     DevTime* d_time = nullptr;
     DevTime* h_time = nullptr;       // pinned
     cudaGraphExec_t graph = nullptr;
@@ -83,11 +86,17 @@ struct lulesh_dev {
     int32_t nx = 0;                  // edge of the cube (Domain::sizeX)
     double* d_verify = nullptr;      // [4] lulesh_dev_verify output (arena)
     double* h_verify = nullptr;      // [4] pinned
-    // lulesh_leapfrog's second copy stream and its hand-off events (created on first use)
-    cudaStream_t cstream = nullptr;
-    cudaEvent_t ev_up = nullptr, ev_e = nullptr, ev_nodes = nullptr, ev_kin = nullptr;
-    std::vector<cudaEvent_t> ev_slab, ev_mat;  // one per slab: upload done, material done
-    cudaStream_t mstream = nullptr;            // downloads of the material phase's outputs
+    // lulesh_leapfrog's upload and download streams and its hand-off events
+    // (created on first use)
+    cudaStream_t cstream = nullptr;  // uploads
+    cudaStream_t mstream = nullptr;  // downloads of the compute stream's results
+    cudaStream_t stream2 = nullptr;  // second compute stream: every other slab
+    cudaStream_t mstream2 = nullptr; // downloads of the second compute stream's results
+    cudaEvent_t ev_up = nullptr, ev_e = nullptr, ev_s2 = nullptr, ev_join = nullptr;
+    // one per slab: upload, mirror (mixed), node range, kinematics and material done
+    std::vector<cudaEvent_t> ev_slab, ev_mir, ev_node, ev_kin, ev_mat;
+    int32_t* upload_flag = nullptr;  // [kLeapfrogSlabs] per-slab "host changed a coordinate" (arena)
+    StepResult* slab_result = nullptr;  // [kLeapfrogSlabs] per material slab: dt minima and block counter
     int32_t* matOrderSlab = nullptr;           // [N_e] slab-major material order (arena)
     Launchers L{};
     // m.geo holds the geometry of the current coordinates (set by the
@@ -213,11 +222,15 @@ void carve_mesh(Mesh& m, Arena& a, int precision, int ne, int nn) {
 void layout(lulesh_dev* d, Arena& a, int ne, int nn, int matGrid) {
     Mesh& m = d->m;
     carve_mesh(m, a, d->precision, ne, nn);
-    // one partial per block of the material launch: the full grid, or a
-    // slab launch of lulesh_leapfrog with one thread per element
-    m.partials = a.take<lulesh::DtPartial>(std::max(matGrid, lulesh::blocks_for(ne, lulesh::kMatBlock)));
+    // one partial per block of the material launch: the full grid, or the
+    // slab launches of lulesh_leapfrog with one thread per element, each in
+    // its own part (at most one block more per slab than one launch over all)
+    m.partials = a.take<lulesh::DtPartial>(
+        std::max(matGrid, lulesh::blocks_for(ne, lulesh::kMatBlock) + kLeapfrogSlabs));
     m.result = a.take<StepResult>(1);
     for (double*& p : d->stage) p = d->L.forces_geo ? a.take<double>(nn) : nullptr;
+    d->upload_flag = a.take<int32_t>(kLeapfrogSlabs);
+    d->slab_result = a.take<StepResult>(kLeapfrogSlabs);
     d->d_time = a.take<DevTime>(1);
     d->d_verify = a.take<double>(4);
     d->matOrderSlab = a.take<int32_t>(ne);
@@ -437,7 +450,8 @@ int new_handle(int32_t precision, int ne, int nn, lulesh_dev** out) {
     m.dtime = nullptr;
     if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(LULESH_ECUDA);
-    if (cudaMallocHost(&d->h_result, sizeof(StepResult)) != cudaSuccess) return fail(LULESH_ENOMEM);
+    if (cudaMallocHost(&d->h_result, sizeof(StepResult) * (1 + kLeapfrogSlabs)) != cudaSuccess)
+        return fail(LULESH_ENOMEM);
     if (cudaMallocHost(&d->h_time, sizeof(DevTime)) != cudaSuccess) return fail(LULESH_ENOMEM);
     if (cudaMallocHost(&d->h_verify, 4 * sizeof(double)) != cudaSuccess) return fail(LULESH_ENOMEM);
     if (cudaMemsetAsync(m.result, 0, sizeof(StepResult), d->stream) != cudaSuccess)
@@ -506,10 +520,15 @@ void lulesh_dev_destroy(lulesh_dev* d) {
     if (d->h_time) cudaFreeHost(d->h_time);
     if (d->h_verify) cudaFreeHost(d->h_verify);
     if (d->cstream) cudaStreamSynchronize(d->cstream);
-    for (cudaEvent_t e : {d->ev_up, d->ev_e, d->ev_nodes, d->ev_kin})
+    for (cudaEvent_t e : {d->ev_up, d->ev_e, d->ev_s2, d->ev_join})
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : d->ev_slab) cudaEventDestroy(e);
-    for (cudaEvent_t e : d->ev_mat) cudaEventDestroy(e);
+    for (auto* evs : {&d->ev_slab, &d->ev_mir, &d->ev_node, &d->ev_kin, &d->ev_mat})
+        for (cudaEvent_t e : *evs) cudaEventDestroy(e);
+    for (cudaStream_t st : {d->stream2, d->mstream2}) {
+        if (!st) continue;
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
     if (d->mstream) {
         cudaStreamSynchronize(d->mstream);
         cudaStreamDestroy(d->mstream);
@@ -576,8 +595,8 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
         return LULESH_EINVAL;
     if (!(v->time->deltatime > 0.0)) return LULESH_EINVAL;
     // The coordinates come from the host buffers. With the geometry form they
-    // upload into copies, and elements whose corners the host left as the
-    // previous step made them reuse the geometry that step stored.
+    // upload into copies, and slabs whose nodes the host left as the previous
+    // step made them reuse the geometry that step stored.
     const bool geo = d->L.forces_geo != nullptr;
     const bool have_geo = geo && d->geo_valid;
     d->geo_valid = false;
@@ -591,47 +610,120 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     if (!d->cstream) {
         CK(cudaStreamCreateWithFlags(&d->cstream, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&d->mstream, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&d->ev_up, &d->ev_e, &d->ev_nodes, &d->ev_kin})
+        CK(cudaStreamCreateWithFlags(&d->stream2, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&d->mstream2, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&d->ev_up, &d->ev_e, &d->ev_s2, &d->ev_join})
             CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     const Mesh& m = d->m;
     const double dt = v->time->deltatime;
     // The cycle runs in slabs of whole element planes (the handle's matOrder
-    // is slab-major). The upload runs slab by slab on the copy stream, and
-    // the force kernel of a slab starts once its elements' inputs and its
-    // nodes (its planes and the next node plane) are on the device, so most
-    // of the upload overlaps the force phase; the energy, read only by the
-    // material phase, uploads last. The fields each phase leaves final go
-    // back while the later phases run: node fields after the node kernel and
-    // kinematic fields after the kinematics kernel (copy stream), each slab's
-    // material outputs after its material launch (third stream).
+    // is slab-major), on five streams: uploads (cstream), compute (stream,
+    // and stream2 for every other slab, so that the tail of one slab's
+    // launch overlaps the next) and downloads (mstream for the results of
+    // stream, mstream2 for those of stream2, so that each goes down as soon
+    // as it is ready).
+    // The host<->device link (about 190 GB/s each way on GB300's C2C,
+    // against 930 MB a cycle at s=150) paces the call as much as the GPU
+    // does, so every transfer overlaps a phase:
+    //   upload slab k (its elements' inputs and its nodes: its planes and the
+    //     next node plane; the energy, read only by the material phase, last)
+    //     -> forces of slab k;
+    //   node update in ranges, one after every two force slabs (the node
+    //     planes below the next slab's, whose corner forces are then all
+    //     formed) and the rest after the last, each range's fields going
+    //     down behind it during the force phase;
+    //   kinematics in slabs of two force slabs, each one's fields going down
+    //     while the next runs, so that they are down before the material
+    //     phase's fields are ready;
+    //   material slab by slab on both compute streams, each slab's fields
+    //     going down behind it; each slab lowers its own dt minima (its own
+    //     block partials and counter), folded on the host at the end.
     const int s = d->nx;
     const int slabs = slab_count(s, m.numElem);
     const bool cube = slabs > 1 || (s >= 1 && int64_t(s) * s * s == int64_t(m.numElem));
     const int64_t plane_n = cube ? int64_t(s + 1) * (s + 1) : m.numNode;
     const int64_t plane_e = cube ? int64_t(s) * s : m.numElem;
     if (d->ev_slab.size() < size_t(slabs)) {
-        for (auto* evs : {&d->ev_slab, &d->ev_mat}) {
+        for (auto* evs : {&d->ev_slab, &d->ev_mir, &d->ev_node, &d->ev_kin, &d->ev_mat}) {
             for (cudaEvent_t e : *evs) cudaEventDestroy(e);
             evs->assign(slabs, nullptr);
             for (cudaEvent_t& e : *evs) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
     }
-    std::vector<int64_t> e_lo(slabs), e_hi(slabs), n_hi(slabs);
+    // elements [e_lo, e_hi) and the nodes of their corners [n_lo, n_hi) of each slab
+    std::vector<int64_t> e_lo(slabs), e_hi(slabs), n_lo(slabs), n_hi(slabs);
     for (int sl = 0; sl < slabs; ++sl) {
         int p0 = 0, p1 = 1;
         if (cube) slab_planes(s, slabs, sl, p0, p1);
         e_lo[sl] = cube ? p0 * plane_e : 0;
         e_hi[sl] = cube ? p1 * plane_e : m.numElem;
+        n_lo[sl] = cube ? p0 * plane_n : 0;
         n_hi[sl] = cube ? (p1 + 1) * plane_n : m.numNode;
     }
     CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
-    // the copy stream starts after the previous cycle's work on the compute stream
+    if (have_geo) CK(cudaMemsetAsync(d->upload_flag, 0, sizeof(int32_t) * slabs, d->stream));
+    CK(cudaMemsetAsync(d->slab_result, 0, sizeof(StepResult) * slabs, d->stream));
+    // the copy streams start after the previous cycle's work on the compute stream
     CK(cudaEventRecord(d->ev_up, d->stream));
     CK(cudaStreamWaitEvent(d->cstream, d->ev_up, 0));
+    CK(cudaStreamWaitEvent(d->mstream, d->ev_up, 0));
+    CK(cudaStreamWaitEvent(d->stream2, d->ev_up, 0));
+    CK(cudaStreamWaitEvent(d->mstream2, d->ev_up, 0));
+
+    // Element fields [e0, e1) in `out` go down once the work queued so far on
+    // compute stream st is done (event ev), on st's download stream.
+    auto elem_down = [&](const std::vector<Copy>& out, int64_t e0, int64_t e1, cudaEvent_t ev,
+                         cudaStream_t st) -> int {
+        cudaStream_t down = st == d->stream2 ? d->mstream2 : d->mstream;
+        CK(cudaEventRecord(ev, st));
+        CK(cudaStreamWaitEvent(down, ev, 0));
+        const size_t off = size_t(e0), cnt = size_t(e1 - e0);
+        for (const Copy& c : out)
+            CK(cudaMemcpyAsync(static_cast<double*>(const_cast<void*>(c.host)) + off,
+                               static_cast<const double*>(c.dev) + off, sizeof(double) * cnt,
+                               cudaMemcpyDeviceToHost, down));
+        return LULESH_OK;
+    };
+
+    // Node update of nodes [a, b) on the compute stream after both compute
+    // streams' work so far, then those node fields go down. With the
+    // geometry form the positions advanced are the uploaded copies.
+    auto node_range = [&](int64_t a, int64_t b, cudaEvent_t ev) -> int {
+        CK(cudaEventRecord(d->ev_s2, d->stream2));
+        CK(cudaStreamWaitEvent(d->stream, d->ev_s2, 0));
+        Mesh mn = m;  // nodes [a, b) as a mesh of b - a nodes at offset a
+        mn.numNode = int(b - a);
+        for (double** f : {&mn.x, &mn.y, &mn.z, &mn.xd, &mn.yd, &mn.zd, &mn.xdd, &mn.ydd, &mn.zdd, &mn.fx,
+                           &mn.fy, &mn.fz})
+            *f += a;
+        mn.nodalMass += a;
+        mn.invMass += a;
+        mn.nodeSymm += a;
+        mn.nodeElemStart += a;
+        if (mn.pxp)
+            for (float2** f : {&mn.pxp, &mn.pyp, &mn.pzp, &mn.vxp, &mn.vyp, &mn.vzp}) *f += a;
+        d->launches += geo ? lulesh::fp64::launch_nodes_upload(mn, dt, d->stage[0] + a, d->stage[1] + a,
+                                                               d->stage[2] + a, d->stream)
+                           : d->L.nodes(mn, dt, d->stream);
+        CK(cudaEventRecord(ev, d->stream));
+        CK(cudaStreamWaitEvent(d->mstream, ev, 0));
+        for (const Copy& c : out_nodes)
+            CK(cudaMemcpyAsync(static_cast<double*>(const_cast<void*>(c.host)) + a,
+                               static_cast<const double*>(c.dev) + a, sizeof(double) * size_t(b - a),
+                               cudaMemcpyDeviceToHost, d->mstream));
+        return LULESH_OK;
+    };
+    int64_t node_next = 0;  // first node not yet updated
+    int nranges = 0;
+
     const Copy* e_in = nullptr;
     int64_t node_done = 0;
     for (int sl = 0; sl < slabs; ++sl) {
+        if (cube && sl > 0 && (sl & 1) == 0) {  // the node planes below slab sl's
+            if (int st = node_range(node_next, n_lo[sl], d->ev_node[nranges++])) return st;
+            node_next = n_lo[sl];
+        }
         const int64_t e0 = e_lo[sl], e1 = e_hi[sl], n1 = n_hi[sl];
         for (const Copy& c : in) {
             if (c.dev == m.e) {
@@ -651,61 +743,85 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
                                    cudaMemcpyHostToDevice, d->cstream));
         }
         CK(cudaEventRecord(d->ev_slab[sl], d->cstream));
-        CK(cudaStreamWaitEvent(d->stream, d->ev_slab[sl], 0));
-        if (d->precision == LULESH_MIXED)
-            d->launches += lulesh::mixed::launch_mirror_range(m, int(node_done), int(n1), d->stream);
-        if (geo)
-            d->launches += lulesh::fp64::launch_forces_stage_range(m, d->stage[0], d->stage[1], d->stage[2], int(e0),
-                                                                   int(e1), have_geo, d->stream);
-        else
-            d->launches += d->L.forces_range(m, int(e0), int(e1), d->stream);
+        cudaStream_t cs = (sl & 1) ? d->stream2 : d->stream;
+        CK(cudaStreamWaitEvent(cs, d->ev_slab[sl], 0));
+        if (d->precision == LULESH_MIXED) {
+            // float-pair mirrors of the slab's new nodes; its first node
+            // plane's come from the previous slab's mirror launch
+            d->launches += lulesh::mixed::launch_mirror_range(m, int(node_done), int(n1), cs);
+            CK(cudaEventRecord(d->ev_mir[sl], cs));
+            if (sl > 0) CK(cudaStreamWaitEvent(cs, d->ev_mir[sl - 1], 0));
+        }
+        if (geo && have_geo) {
+            // the slab's nodes against the device's own: the stored geometry
+            // where none changed, else the geometry of the uploaded values
+            int32_t* flag = d->upload_flag + sl;
+            d->launches += lulesh::fp64::launch_upload_check(m, d->stage[0], d->stage[1], d->stage[2],
+                                                             int(n_lo[sl]), int(n1), flag, cs);
+            d->launches += lulesh::fp64::launch_forces_geo_unless(m, int(e0), int(e1), flag, cs);
+            d->launches += lulesh::fp64::launch_forces_upload(m, d->stage[0], d->stage[1], d->stage[2], int(e0),
+                                                              int(e1), flag, cs);
+        } else if (geo) {
+            d->launches += lulesh::fp64::launch_forces_upload(m, d->stage[0], d->stage[1], d->stage[2], int(e0),
+                                                              int(e1), nullptr, cs);
+        } else {
+            d->launches += d->L.forces_range(m, int(e0), int(e1), cs);
+        }
         node_done = n1;
     }
-    if (geo) {  // the uploaded coordinates become the device's (after every slab compared them)
-        double* cur[3] = {m.x, m.y, m.z};
-        for (int k = 0; k < 3; ++k)
-            CK(cudaMemcpyAsync(cur[k], d->stage[k], sizeof(double) * size_t(m.numNode), cudaMemcpyDeviceToDevice,
-                               d->stream));
-    }
+
     if (e_in) CK(cudaMemcpyAsync(e_in->dev, e_in->host, e_in->bytes, cudaMemcpyHostToDevice, d->cstream));
     CK(cudaEventRecord(d->ev_e, d->cstream));
-    d->launches += d->L.nodes(m, dt, d->stream);
-    CK(cudaEventRecord(d->ev_nodes, d->stream));
-    d->launches += geo ? d->L.kinematics_geo(m, dt, d->stream) : d->L.kinematics(m, dt, d->stream);
-    CK(cudaEventRecord(d->ev_kin, d->stream));
-    CK(cudaStreamWaitEvent(d->cstream, d->ev_nodes, 0));
-    for (const Copy& c : out_nodes)
-        CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->cstream));
-    CK(cudaStreamWaitEvent(d->cstream, d->ev_kin, 0));
-    for (const Copy& c : out_kin)
-        CK(cudaMemcpyAsync(const_cast<void*>(c.host), c.dev, c.bytes, cudaMemcpyDeviceToHost, d->cstream));
+    if (int st = node_range(node_next, m.numNode, d->ev_node[nranges])) return st;
+    CK(cudaStreamWaitEvent(d->stream2, d->ev_node[nranges], 0));
+    for (int k = 0; k < slabs; k += 2) {
+        const int64_t e0 = e_lo[k], e1 = e_hi[std::min(k + 1, slabs - 1)];
+        cudaStream_t cs = (k & 2) ? d->stream2 : d->stream;
+        d->launches += geo ? d->L.kinematics_geo_range(m, dt, int(e0), int(e1), cs)
+                           : d->L.kinematics_range(m, dt, int(e0), int(e1), cs);
+        if (int st = elem_down(out_kin, e0, e1, d->ev_kin[k], cs)) return st;
+    }
+    // the material phase reads the kinematics of both compute streams (the
+    // Q limiter reads neighbouring elements' gradients) and the energy
+    CK(cudaEventRecord(d->ev_s2, d->stream2));
+    CK(cudaStreamWaitEvent(d->stream, d->ev_s2, 0));
+    CK(cudaEventRecord(d->ev_join, d->stream));
+    CK(cudaStreamWaitEvent(d->stream2, d->ev_join, 0));
     CK(cudaStreamWaitEvent(d->stream, d->ev_e, 0));
+    CK(cudaStreamWaitEvent(d->stream2, d->ev_e, 0));
     Mesh ms = m;  // the slab-major material order: positions [e_lo, e_hi) are the slab's elements
     if (slabs > 1) ms.matOrder = d->matOrderSlab;
+    int part = 0;  // first block partial of the slab
     for (int sl = 0; sl < slabs; ++sl) {
         // one thread per element: blocks schedule dynamically, the slab's
         // most expensive elements first (repeat-count order within a slab)
+        cudaStream_t cs = (sl & 1) ? d->stream2 : d->stream;
         ms.matGrid = std::max(1, lulesh::blocks_for(int(e_hi[sl] - e_lo[sl]), lulesh::kMatBlock));
-        d->launches += d->L.material_range(ms, int(e_lo[sl]), int(e_hi[sl]), sl > 0, d->stream);
-        CK(cudaEventRecord(d->ev_mat[sl], d->stream));
-        CK(cudaStreamWaitEvent(d->mstream, d->ev_mat[sl], 0));
-        const size_t off = size_t(e_lo[sl]), cnt = size_t(e_hi[sl] - e_lo[sl]);
-        for (const Copy& c : out_mat)
-            CK(cudaMemcpyAsync(const_cast<double*>(static_cast<const double*>(c.host)) + off,
-                               static_cast<double*>(c.dev) + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost,
-                               d->mstream));
+        ms.partials = m.partials + part;
+        ms.result = d->slab_result + sl;
+        part += ms.matGrid;
+        d->launches += d->L.material_range(ms, int(e_lo[sl]), int(e_hi[sl]), false, cs);
+        if (int st = elem_down(out_mat, e_lo[sl], e_hi[sl], d->ev_mat[sl], cs)) return st;
     }
     CK(cudaGetLastError());
+    CK(cudaEventRecord(d->ev_s2, d->stream2));
+    CK(cudaStreamWaitEvent(d->stream, d->ev_s2, 0));
     CK(cudaMemcpyAsync(d->h_result, m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
-    CK(cudaStreamSynchronize(d->stream));
-    CK(cudaStreamSynchronize(d->cstream));
-    CK(cudaStreamSynchronize(d->mstream));
+    CK(cudaMemcpyAsync(d->h_result + 1, d->slab_result, sizeof(StepResult) * slabs, cudaMemcpyDeviceToHost,
+                       d->stream));
+    for (cudaStream_t st : {d->stream, d->cstream, d->mstream, d->mstream2}) CK(cudaStreamSynchronize(st));
     if (d->h_result->err != 0) {
         d->err_elem = d->h_result->err_elem;
         return d->h_result->err;
     }
-    v->time->dtcourant = d->h_result->dtcourant;
-    v->time->dthydro = d->h_result->dthydro;
+    // the step's minima: the least of the slabs' (exact, so in any order)
+    double dtc = d->h_result[1].dtcourant, dth = d->h_result[1].dthydro;
+    for (int sl = 1; sl < slabs; ++sl) {
+        dtc = std::min(dtc, d->h_result[1 + sl].dtcourant);
+        dth = std::min(dth, d->h_result[1 + sl].dthydro);
+    }
+    v->time->dtcourant = dtc;
+    v->time->dthydro = dth;
     d->geo_valid = geo;
     return LULESH_OK;
 }

@@ -235,31 +235,21 @@ __device__ __forceinline__ void forces_geo_elem(const Mesh& m, int i) {
     forces_from_geo(m, i, nl, g);
 }
 
-// Forces of element i in lulesh_leapfrog: the coordinates just uploaded from
-// the host (sx, sy, sz) are the step's; where they equal, bit for bit, the
-// device's own coordinates at all 8 corners (the previous step's results, the
-// host having left them unchanged) and the stored geometry is that of the
-// device's coordinates (have_geo), the stored geometry is used, else it is
-// formed from the uploaded coordinates.
-__device__ __forceinline__ void forces_stage_elem(const Mesh& m, const double* __restrict__ sx,
-                                                  const double* __restrict__ sy,
-                                                  const double* __restrict__ sz, int i, bool have_geo) {
+// Forces of element i in lulesh_leapfrog with the geometry formed from the
+// coordinates just uploaded from the host (sx, sy, sz), the step's own.
+__device__ __forceinline__ void forces_upload_elem(const Mesh& m, const double* __restrict__ sx,
+                                                   const double* __restrict__ sy,
+                                                   const double* __restrict__ sz, int i) {
     int nl[8];
     load_nodelist(m.nodelist, i, nl);
-    double x[8], y[8], z[8];
-    gather8(sx, nl, x);
-    gather8(sy, nl, y);
-    gather8(sz, nl, z);
-    bool same = have_geo;
-    if (same) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            same = same && dbits(x[k]) == dbits(LD(m.x + nl[k])) && dbits(y[k]) == dbits(LD(m.y + nl[k])) &&
-                   dbits(z[k]) == dbits(LD(m.z + nl[k]));
-    }
     ElemGeo g;
-    if (same) geo_load(m, i, g);
-    else elem_geometry(x, y, z, g);
+    {
+        double x[8], y[8], z[8];
+        gather8(sx, nl, x);
+        gather8(sy, nl, y);
+        gather8(sz, nl, z);
+        elem_geometry(x, y, z, g);
+    }
     forces_from_geo(m, i, nl, g);
 }
 
@@ -278,8 +268,10 @@ __device__ __forceinline__ void geometry_elem(const Mesh& m, int i) {
 #endif
 
 // Node n: gather in CSR order, stress then hourglass per corner
-// (combineVolumeForcesTaskFunc, lulesh.cc:838-862), then the node update.
-__device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt) {
+// (combineVolumeForcesTaskFunc, lulesh.cc:838-862), then the node update
+// (of positions px, py, pz when given, see node_update).
+__device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt, const double* px = nullptr,
+                                           const double* py = nullptr, const double* pz = nullptr) {
     const size_t N = (size_t)m.numElem;
     const int b = LD(m.nodeElemStart + n), e = LD(m.nodeElemStart + n + 1);
     double fx = 0.0, fy = 0.0, fz = 0.0;
@@ -299,7 +291,7 @@ __device__ __forceinline__ void nodes_node(const Mesh& m, int n, double dt) {
         fz += LD(m.fsz + idx);
 #endif
     }
-    node_update(m, n, fx, fy, fz, dt);
+    node_update(m, n, fx, fy, fz, dt, px, py, pz);
 }
 
 // CalcKinematicsForElemsTask (lulesh.cc:1169-1275) and
@@ -420,13 +412,15 @@ __global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
     if (n < m.numNode) nodes_node(m, n, dt);
 }
 
-__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
+// all elements, or (RANGED) elements [first, end)
+template <bool RANGED>
+__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt, int first, int end) {
     if (m.dtime) {
         if (!m.dtime->active) return;
         dt = m.dtime->deltatime;
     }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m.numElem) kinematics_elem(m, i, dt);
+    const int i = (RANGED ? first : 0) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < (RANGED ? end : m.numElem)) kinematics_elem(m, i, dt);
 }
 
 #if !LULESH_EXACT
@@ -440,19 +434,54 @@ __global__ void __launch_bounds__(kForceBlock) k_forces_geo(Mesh m) {
 // At least 3 blocks of 128 per SM (at most 168 registers): with the
 // integer-pipe products the compiler's own choice, 240 registers and 2
 // blocks, left the FP64 pipe waiting (2.09 -> 2.00 ms at s=150).
-__global__ void __launch_bounds__(kKinBlock, 3) k_kinematics_geo(Mesh m, double dt) {
+template <bool RANGED>
+__global__ void __launch_bounds__(kKinBlock, 3) k_kinematics_geo(Mesh m, double dt, int first, int end) {
     if (m.dtime) {
         if (!m.dtime->active) return;
         dt = m.dtime->deltatime;
     }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m.numElem) kinematics_fast<true>(m, i, dt);
+    const int i = (RANGED ? first : 0) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < (RANGED ? end : m.numElem)) kinematics_fast<true>(m, i, dt);
 }
-__global__ void __launch_bounds__(kForceBlock) k_forces_stage(Mesh m, const double* sx, const double* sy,
-                                                               const double* sz, int first, int end,
-                                                               int have_geo) {
+
+// lulesh_leapfrog's check of one slab: *flag = 1 when the host's uploaded
+// coordinates (sx, sy, sz) of a node in [first, end) differ, bit for bit,
+// from the device's own (the previous step's results). Every thread of a
+// warp reaches the vote; the flag starts at 0 (cleared by the host call).
+__global__ void __launch_bounds__(kNodeBlock) k_upload_check(Mesh m, const double* sx, const double* sy,
+                                                              const double* sz, int first, int end, int* flag) {
+    const int n = first + blockIdx.x * blockDim.x + threadIdx.x;
+    bool differs = false;
+    if (n < end)
+        differs = dbits(LD(sx + n)) != dbits(LD(m.x + n)) || dbits(LD(sy + n)) != dbits(LD(m.y + n)) ||
+                  dbits(LD(sz + n)) != dbits(LD(m.z + n));
+    if (__any_sync(0xffffffffu, differs) && (threadIdx.x & 31) == 0) *flag = 1;
+}
+// lulesh_leapfrog's node phase: every node, the positions advanced being the
+// uploaded copies sx, sy, sz (the step's own coordinates).
+__global__ void __launch_bounds__(kNodeBlock) k_nodes_upload(Mesh m, double dt, const double* sx,
+                                                              const double* sy, const double* sz) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < m.numNode) nodes_node(m, n, dt, sx, sy, sz);
+}
+// Forces of elements [first, end) from the stored geometry, unless the
+// slab's check found a changed node (*flag).
+__global__ void __launch_bounds__(kForceBlock) k_forces_geo_unless(Mesh m, int first, int end,
+                                                                    const int* flag) {
+    if (*flag) return;
     const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < end) forces_stage_elem(m, sx, sy, sz, i, have_geo != 0);
+    if (i < end) forces_geo_elem(m, i);
+}
+// Forces of elements [first, end) with the geometry formed from the uploaded
+// coordinates: always (flag null) or when the slab's check found a changed
+// node (*flag). The two kernels give the same bits for an unchanged element
+// (the stored geometry is formed by the same function from the same values).
+__global__ void __launch_bounds__(kForceBlock) k_forces_upload(Mesh m, const double* sx, const double* sy,
+                                                                const double* sz, int first, int end,
+                                                                const int* flag) {
+    if (flag && !*flag) return;
+    const int i = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < end) forces_upload_elem(m, sx, sy, sz, i);
 }
 __global__ void __launch_bounds__(kForceBlock) k_geometry(Mesh m) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -487,7 +516,12 @@ int launch_nodes(const Mesh& m, double dt, cudaStream_t s) {
     return 1;
 }
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s) {
-    k_kinematics<<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt);
+    k_kinematics<false><<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt, 0, m.numElem);
+    return 1;
+}
+int launch_kinematics_range(const Mesh& m, double dt, int first, int end, cudaStream_t s) {
+    if (end <= first) return 0;
+    k_kinematics<true><<<blocks_for(end - first, kKinBlock), kKinBlock, 0, s>>>(m, dt, first, end);
     return 1;
 }
 int launch_material(const Mesh& m, cudaStream_t s) {
@@ -504,14 +538,34 @@ int launch_forces_geo(const Mesh& m, cudaStream_t s) {
     return 1;
 }
 int launch_kinematics_geo(const Mesh& m, double dt, cudaStream_t s) {
-    k_kinematics_geo<<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt);
+    k_kinematics_geo<false><<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt, 0, m.numElem);
     return 1;
 }
-int launch_forces_stage_range(const Mesh& m, const double* sx, const double* sy, const double* sz, int first,
-                              int end, bool have_geo, cudaStream_t s) {
+int launch_kinematics_geo_range(const Mesh& m, double dt, int first, int end, cudaStream_t s) {
     if (end <= first) return 0;
-    k_forces_stage<<<blocks_for(end - first, kForceBlock), kForceBlock, 0, s>>>(m, sx, sy, sz, first, end,
-                                                                                have_geo ? 1 : 0);
+    k_kinematics_geo<true><<<blocks_for(end - first, kKinBlock), kKinBlock, 0, s>>>(m, dt, first, end);
+    return 1;
+}
+int launch_nodes_upload(const Mesh& m, double dt, const double* sx, const double* sy, const double* sz,
+                        cudaStream_t s) {
+    k_nodes_upload<<<blocks_for(m.numNode, kNodeBlock), kNodeBlock, 0, s>>>(m, dt, sx, sy, sz);
+    return 1;
+}
+int launch_upload_check(const Mesh& m, const double* sx, const double* sy, const double* sz, int first, int end,
+                        int32_t* flag, cudaStream_t s) {
+    if (end <= first) return 0;
+    k_upload_check<<<blocks_for(end - first, kNodeBlock), kNodeBlock, 0, s>>>(m, sx, sy, sz, first, end, flag);
+    return 1;
+}
+int launch_forces_geo_unless(const Mesh& m, int first, int end, const int32_t* flag, cudaStream_t s) {
+    if (end <= first) return 0;
+    k_forces_geo_unless<<<blocks_for(end - first, kForceBlock), kForceBlock, 0, s>>>(m, first, end, flag);
+    return 1;
+}
+int launch_forces_upload(const Mesh& m, const double* sx, const double* sy, const double* sz, int first, int end,
+                         const int32_t* flag, cudaStream_t s) {
+    if (end <= first) return 0;
+    k_forces_upload<<<blocks_for(end - first, kForceBlock), kForceBlock, 0, s>>>(m, sx, sy, sz, first, end, flag);
     return 1;
 }
 int launch_geometry(const Mesh& m, cudaStream_t s) {

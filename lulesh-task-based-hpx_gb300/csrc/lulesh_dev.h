@@ -116,6 +116,7 @@ int launch_forces(const Mesh& m, cudaStream_t s);
 int launch_forces_range(const Mesh& m, int first, int end, cudaStream_t s);  // elements [first, end)
 int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
+int launch_kinematics_range(const Mesh& m, double dt, int first, int end, cudaStream_t s);  // elements
 int launch_material(const Mesh& m, cudaStream_t s);
 // matOrder positions [first, end); accumulate: fold the dt minima into m.result's
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
@@ -124,18 +125,28 @@ int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cu
 // forms it from the current coordinates when it is stale
 int launch_forces_geo(const Mesh& m, cudaStream_t s);
 int launch_kinematics_geo(const Mesh& m, double dt, cudaStream_t s);
+int launch_kinematics_geo_range(const Mesh& m, double dt, int first, int end, cudaStream_t s);
 int launch_geometry(const Mesh& m, cudaStream_t s);
-// lulesh_leapfrog's force phase over elements [first, end): coordinates from
-// the uploaded copies sx, sy, sz, stored geometry where they match m.x, m.y,
-// m.z and have_geo
-int launch_forces_stage_range(const Mesh& m, const double* sx, const double* sy, const double* sz, int first,
-                              int end, bool have_geo, cudaStream_t s);
+// lulesh_leapfrog's force phase, slab by slab: the check of the slab's nodes
+// [first, end) (*flag = 1 when an uploaded coordinate sx, sy, sz differs from
+// m.x, m.y, m.z), then forces of its elements [first, end) from the stored
+// geometry unless *flag, and forces with the geometry formed from the
+// uploaded coordinates when *flag (always when flag is null)
+int launch_upload_check(const Mesh& m, const double* sx, const double* sy, const double* sz, int first, int end,
+                        int32_t* flag, cudaStream_t s);
+int launch_forces_geo_unless(const Mesh& m, int first, int end, const int32_t* flag, cudaStream_t s);
+// and its node phase: positions advanced from the uploaded copies
+int launch_nodes_upload(const Mesh& m, double dt, const double* sx, const double* sy, const double* sz,
+                        cudaStream_t s);
+int launch_forces_upload(const Mesh& m, const double* sx, const double* sy, const double* sz, int first, int end,
+                         const int32_t* flag, cudaStream_t s);
 }  // namespace fp64
 namespace fp64x {
 int launch_forces(const Mesh& m, cudaStream_t s);
 int launch_forces_range(const Mesh& m, int first, int end, cudaStream_t s);  // elements [first, end)
 int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
+int launch_kinematics_range(const Mesh& m, double dt, int first, int end, cudaStream_t s);  // elements
 int launch_material(const Mesh& m, cudaStream_t s);
 // matOrder positions [first, end); accumulate: fold the dt minima into m.result's
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);
@@ -145,6 +156,7 @@ int launch_forces(const Mesh& m, cudaStream_t s);
 int launch_forces_range(const Mesh& m, int first, int end, cudaStream_t s);  // elements [first, end)
 int launch_nodes(const Mesh& m, double dt, cudaStream_t s);
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s);
+int launch_kinematics_range(const Mesh& m, double dt, int first, int end, cudaStream_t s);  // elements
 int launch_material(const Mesh& m, cudaStream_t s);
 // matOrder positions [first, end); accumulate: fold the dt minima into m.result's
 int launch_material_range(const Mesh& m, int first, int end, bool accumulate, cudaStream_t s);

@@ -204,13 +204,15 @@ __global__ void __launch_bounds__(kNodeBlock) k_nodes(Mesh m, double dt) {
     if (n < m.numNode) nodes_node(m, n, dt);
 }
 
-__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt) {
+// all elements, or (RANGED) elements [first, end)
+template <bool RANGED>
+__global__ void __launch_bounds__(kKinBlock) k_kinematics(Mesh m, double dt, int first, int end) {
     if (m.dtime) {
         if (!m.dtime->active) return;
         dt = m.dtime->deltatime;
     }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m.numElem) kinematics_elem(m, i, dt);
+    const int i = (RANGED ? first : 0) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < (RANGED ? end : m.numElem)) kinematics_elem(m, i, dt);
 }
 
 __global__ void __launch_bounds__(kMatBlock) k_material(Mesh m, int first, int end, int accumulate) {
@@ -244,7 +246,12 @@ int launch_nodes(const Mesh& m, double dt, cudaStream_t s) {
     return 1;
 }
 int launch_kinematics(const Mesh& m, double dt, cudaStream_t s) {
-    k_kinematics<<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt);
+    k_kinematics<false><<<blocks_for(m.numElem, kKinBlock), kKinBlock, 0, s>>>(m, dt, 0, m.numElem);
+    return 1;
+}
+int launch_kinematics_range(const Mesh& m, double dt, int first, int end, cudaStream_t s) {
+    if (end <= first) return 0;
+    k_kinematics<true><<<blocks_for(end - first, kKinBlock), kKinBlock, 0, s>>>(m, dt, first, end);
     return 1;
 }
 int launch_material(const Mesh& m, cudaStream_t s) {

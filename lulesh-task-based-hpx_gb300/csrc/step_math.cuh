@@ -1313,8 +1313,12 @@ __device__ __forceinline__ void finish_dt_reduction(const Mesh& m, double dtc, d
 
 // Acceleration, symmetry-plane zeroing, velocity with u_cut and position of
 // node n from its gathered force (lulesh.cc:1115-1158, 566-588).
+// The positions advanced are m.x, m.y, m.z, or px, py, pz when given (the
+// drop-in call's uploaded coordinates); the result goes to m.x, m.y, m.z.
 __device__ __forceinline__ void node_update(const Mesh& m, int n, double fx, double fy, double fz,
-                                            double dt) {
+                                            double dt, const double* __restrict__ px = nullptr,
+                                            const double* __restrict__ py = nullptr,
+                                            const double* __restrict__ pz = nullptr) {
     m.fx[n] = fx;
     m.fy[n] = fy;
     m.fz[n] = fz;
@@ -1343,9 +1347,12 @@ __device__ __forceinline__ void node_update(const Mesh& m, int n, double fx, dou
     m.xd[n] = vx;
     m.yd[n] = vy;
     m.zd[n] = vz;
-    m.x[n] = m.x[n] + vx * dt;
-    m.y[n] = m.y[n] + vy * dt;
-    m.z[n] = m.z[n] + vz * dt;
+    const double x0 = px ? LD(px + n) : m.x[n];
+    const double y0 = py ? LD(py + n) : m.y[n];
+    const double z0 = pz ? LD(pz + n) : m.z[n];
+    m.x[n] = x0 + vx * dt;
+    m.y[n] = y0 + vy * dt;
+    m.z[n] = z0 + vz * dt;
 }
 
 // CheckAndUpdateVolumeForElems (lulesh.cc:1252-1272): checks the old v, then

@@ -223,16 +223,18 @@ def test_run_to_run_determinism(lulesh, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp64_exact", "mixed"])
-def test_leapfrog_on_host_buffers_equals_resident_run(lulesh, precision):
+@pytest.mark.parametrize("size", [10, 19])
+def test_leapfrog_on_host_buffers_equals_resident_run(lulesh, precision, size):
     """lulesh_leapfrog (upload, step, download each cycle, the literal
-    drop-in for LagrangeLeapFrog(Domain&), its copies overlapping the
-    cycle) gives the device-resident bits, dt constraints included."""
-    a = lulesh.HostDomain(10)
+    drop-in for LagrangeLeapFrog(Domain&), run slab by slab with its copies
+    overlapping the cycle) gives the device-resident bits, dt constraints
+    included."""
+    a = lulesh.HostDomain(size)
     dev_a = lulesh.Device(a, precision)
     for _ in range(25):
         a.time_increment()
         dev_a.leapfrog()
-    b, _, n = _run_device(lulesh, 10, 11, 1, 1, precision, its=25)
+    b, _, n = _run_device(lulesh, size, 11, 1, 1, precision, its=25)
     assert a.cycle == b.cycle == n == 25
     for f in ("time", "deltatime", "dtcourant", "dthydro"):
         assert getattr(a.time_state, f) == getattr(b.time_state, f), f
@@ -240,14 +242,17 @@ def test_leapfrog_on_host_buffers_equals_resident_run(lulesh, precision):
         np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
 
 
-def test_leapfrog_with_host_changed_coordinates(lulesh):
+# s=10 runs the drop-in call in 8 slabs of element planes [0,1) [1,2) [2,3)
+# [3,5) [5,6) [6,7) [7,8) [8,10); moved nodes: plane 1 (row 1, column 5), the
+# slab boundary plane 5, and the top plane 10 (in the last node range).
+@pytest.mark.parametrize("node", [137, 5 * 121 + 5 * 11 + 5, 10 * 121 + 5 * 11 + 3])
+def test_leapfrog_with_host_changed_coordinates(lulesh, node):
     """lulesh_leapfrog reuses the element geometry its previous step stored
-    only for elements whose 8 corners the host left as that step made them.
-    With one node moved on the host between two calls, the drop-in run stays
-    bit for bit the device-resident run given the same move by upload."""
+    only for slabs whose nodes the host left as that step made them. With
+    one node moved on the host between two calls, the drop-in run stays bit
+    for bit the device-resident run given the same move by upload."""
     a, b = lulesh.HostDomain(10), lulesh.HostDomain(10)
     dev_a, dev_b = lulesh.Device(a, "fp64"), lulesh.Device(b, "fp64")
-    node = 137  # an interior node (plane 1, row 1, column 5 of s=10)
     for cycle in range(12):
         if cycle == 6:
             dev_b.download(lulesh.F_POS)
