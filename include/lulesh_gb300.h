@@ -10,8 +10,9 @@
  *    LULESH_OK or a negative code; LULESH_EVOLUME is the reference's
  *    VolumeError (lulesh.h:30), the condition on which the reference calls
  *    exit(VolumeError) (lulesh.cc:821, 908, 1262).
- *  - A lulesh_dev handle owns one CUDA stream and device copies of every
- *    Domain array the step touches. Use a handle from one host thread at a
+ *  - A lulesh_dev handle owns one CUDA stream (lulesh_leapfrog creates four
+ *    more on its first call) and device copies of every Domain array the
+ *    step touches. Use a handle from one host thread at a
  *    time. Host arrays stay owned by the caller.
  *  - All arithmetic of LULESH_FP64 and LULESH_FP64_EXACT is IEEE double, as
  *    the reference (Real_t = double, lulesh.h:27). LULESH_MIXED runs the
@@ -193,14 +194,17 @@ int lulesh_dev_step(lulesh_dev* dev, double deltatime, double* dtcourant, double
 /* The literal drop-in for LagrangeLeapFrogWithTasks(Domain&): uploads the
  * state a step reads from the host Domain view, runs one cycle with
  * view->time->deltatime, downloads every field the step writes and stores
- * dtcourant/dthydro into view->time. The copies overlap the cycle: the
- * upload runs on two streams, node fields stream back while the element
- * phases run and the kinematic fields while the material phase runs. With
- * LULESH_FP64, elements whose 8 corner coordinates equal those the previous
+ * dtcourant/dthydro into view->time. The cycle runs in slabs of element
+ * planes and the copies overlap it: each slab's inputs upload ahead of its
+ * force kernel, node fields go back behind the node update of each pair of
+ * slabs, element fields behind each kinematics and material slab. With
+ * LULESH_FP64, slabs whose node coordinates all equal those the previous
  * call left on the device reuse the element geometry it stored; the others
- * form it from the uploaded coordinates (same results either way). On
- * LULESH_EVOLUME (where the reference exits) the host fields hold the
- * partly advanced state and view->time's dt constraints are unchanged. */
+ * form it from the uploaded coordinates (same results either way). The
+ * host arrays must stay untouched until the call returns; pin them
+ * (lulesh_domain_pin) for full link bandwidth. On LULESH_EVOLUME (where the
+ * reference exits) the host fields hold the partly advanced state and
+ * view->time's dt constraints are unchanged. */
 int lulesh_leapfrog(lulesh_dev* dev, lulesh_domain_view* host);
 
 /* The time loop of hpx_main (lulesh.cc:2374-2386) on device-resident state:
