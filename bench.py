@@ -327,6 +327,52 @@ def cpu_oracle_rate(s: int, r: int, cycles: int, threads: int) -> tuple[float, f
     return ne * cycles / dt, dt
 
 
+def link_rates(device: int, mb: int = 256, reps: int = 3) -> dict:
+    """Pinned host<->device copy rates of this machine (GB/s, best of reps):
+    device to host, host to device, and both directions at once (half the
+    bytes each way on two streams, total bytes over the time). The drop-in
+    call's copies run over this link."""
+    import torch
+
+    n = (mb << 20) // 8
+    h = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(n, dtype=torch.float64, device=f"cuda:{device}")
+    s1, s2 = torch.cuda.Stream(device), torch.cuda.Stream(device)
+
+    def best(fn):
+        t = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(s1)
+            s2.wait_event(a)
+            fn()
+            s1.wait_stream(s2)
+            b.record(s1)
+            b.synchronize()
+            t.append(a.elapsed_time(b) / 1e3)
+        return n * 8 / min(t) / 1e9
+
+    def d2h():
+        with torch.cuda.stream(s1):
+            h.copy_(d, non_blocking=True)
+
+    def h2d():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+
+    def both():
+        with torch.cuda.stream(s1):
+            h[: n // 2].copy_(d[: n // 2], non_blocking=True)
+        with torch.cuda.stream(s2):
+            d[n // 2:].copy_(h[n // 2:], non_blocking=True)
+
+    out = {"d2h": round(best(d2h), 1), "h2d": round(best(h2d), 1), "both": round(best(both), 1),
+           "bytes": n * 8, "how": "pinned torch copies, CUDA events, best of 3"}
+    del h, d
+    return out
+
+
 def reference_code_rate(s: int, r: int, cycles: int) -> dict | None:
     """The reference's own code on this host: its unmodified lulesh.cc,
     lulesh-init.cc and lulesh-viz.cc built here against the sequential HPX
@@ -400,6 +446,7 @@ def run_ours(args) -> None:
     e2e_value = world * ne * K / e2e_s
     h2d = (6 * nn + 5 * ne) * 8
     d2h = (12 * nn + 11 * ne) * 8 + 16
+    link = link_rates(local)
     dev.close()
     dom.close()
 
@@ -478,7 +525,11 @@ def run_ours(args) -> None:
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "how": "lulesh_leapfrog per cycle: upload step inputs from pinned host arrays, "
-                       "run, download every field the step writes; wall clock"},
+                       "run, download every field the step writes; wall clock",
+                "ms_per_step": round(1e3 * e2e_s / K, 4),
+                "link_gbs": link,
+                "link_floor_ms": round(1e3 * d2h / (link["d2h"] * 1e9), 3),
+                "link_floor_note": "the step's downloads alone at the measured device-to-host rate"},
         "gpu_launches": launches,
         "fom": fom(value),
         "kernel_ms_per_step": {k: round(v / K, 4) for k, v in prof["kernel_ms"].items()},
