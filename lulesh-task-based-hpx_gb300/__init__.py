@@ -427,19 +427,22 @@ def probe_library() -> C.CDLL:
         lib.lulesh_probe_math.restype = C.c_int32
         lib.lulesh_probe_math.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                           C.c_int64]
-        lib.lulesh_probe_dmul.restype = C.c_int32
-        lib.lulesh_probe_dmul.argtypes = [C.POINTER(C.c_double)] * 4 + [C.c_int64]
+        for name in ("lulesh_probe_dmul", "lulesh_probe_dadd"):
+            getattr(lib, name).restype = C.c_int32
+            getattr(lib, name).argtypes = [C.POINTER(C.c_double)] * 4 + [C.c_int64]
         _probe_lib = lib
     return _probe_lib
 
 
 def pipe_rates() -> dict:
     """Measured rates (ops/s) of the current GPU: double FMA, add, divide, sqrt,
-    float FMA, and double multiplies on the FP64 pipe, on the integer pipes
-    (dmul_ipipe) and on both at once."""
-    out = (C.c_double * 8)()
+    float FMA, double multiplies on the FP64 pipe, on the integer pipes
+    (dmul_ipipe) and on both at once, and double adds on the integer pipes
+    (dadd_ipipe) and on both at once."""
+    out = (C.c_double * 10)()
     _check(probe_library().lulesh_probe_pipe_rates(out), "lulesh_probe_pipe_rates")
-    return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma", "dmul", "dmul_ipipe", "dmul_both"), list(out)))
+    return dict(zip(("dfma", "dadd", "ddiv", "dsqrt", "ffma", "dmul", "dmul_ipipe", "dmul_both", "dadd_ipipe",
+                     "dadd_both"), list(out)))
 
 
 MATH_FUNCTIONS = {"rcp": 0, "rcbrt": 1, "sqrt": 2, "rsqrt": 3, "rcp_seed": 4, "narrow": 5, "split_hi": 6,
@@ -459,17 +462,26 @@ def probe_math(fn: str, x):
     return out
 
 
-def probe_dmul(a, b):
-    """The products a * b on the device by the FP64 pipe's multiply and by the
-    integer-pipe multiply the step kernels use; returns (native, ipipe)."""
+def _probe_pair(name: str, a, b):
     a = np.ascontiguousarray(a, dtype=np.float64)
     b = np.ascontiguousarray(b, dtype=np.float64)
     native, ipipe = np.empty_like(a), np.empty_like(a)
     pd = C.POINTER(C.c_double)
-    _check(probe_library().lulesh_probe_dmul(a.ctypes.data_as(pd), b.ctypes.data_as(pd),
-                                             native.ctypes.data_as(pd), ipipe.ctypes.data_as(pd), a.size),
-           "lulesh_probe_dmul")
+    _check(getattr(probe_library(), name)(a.ctypes.data_as(pd), b.ctypes.data_as(pd),
+                                          native.ctypes.data_as(pd), ipipe.ctypes.data_as(pd), a.size), name)
     return native, ipipe
+
+
+def probe_dmul(a, b):
+    """The products a * b on the device by the FP64 pipe's multiply and by the
+    integer-pipe multiply the step kernels use; returns (native, ipipe)."""
+    return _probe_pair("lulesh_probe_dmul", a, b)
+
+
+def probe_dadd(a, b):
+    """The sums a + b on the device by the FP64 pipe's add and by the
+    integer-pipe add of the probes (dadd_ipipe); returns (native, ipipe)."""
+    return _probe_pair("lulesh_probe_dadd", a, b)
 
 
 def serve(requests: list[dict], precision: str = "mixed", hbm_budget: int = 160 << 30,

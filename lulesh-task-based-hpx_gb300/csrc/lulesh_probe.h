@@ -17,9 +17,10 @@ extern "C" {
  * add/s, out[2] double divide/s, out[3] double square root/s, out[4] float
  * FMA/s, out[5] double multiplies/s on the FP64 pipe, out[6] the same on the
  * integer pipes (the step's dmul_ipipe), out[7] both at once (half of the
- * chains each); per-thread operations. The double path is bound by out[0];
- * takes about 60 ms. Returns 0 or a LULESH_* status. */
-int lulesh_probe_pipe_rates(double out[8]);
+ * chains each), out[8] double adds/s on the integer pipes (dadd_ipipe),
+ * out[9] adds on both at once; per-thread operations. The double path is
+ * bound by out[0]; takes about 80 ms. Returns 0 or a LULESH_* status. */
+int lulesh_probe_pipe_rates(double out[10]);
 
 /* Evaluates one arithmetic helper of the fast variants on the device for n
  * inputs (accuracy tests compare the results with correctly rounded host
@@ -34,6 +35,12 @@ int lulesh_probe_math(int32_t fn, const double* in, double* out, int64_t n);
  * multiply (native) and by the step's integer-pipe multiply (ipipe, which
  * must give the same bits). n <= 2^26. */
 int lulesh_probe_dmul(const double* a, const double* b, double* native, double* ipipe, int64_t n);
+
+/* The double sum of a[i] and b[i] for n pairs, by the FP64 pipe's add
+ * (native) and by an integer-pipe add (dadd_ipipe, which must give the same
+ * bits; measured slower than the FP64 pipe's, so no step kernel uses it).
+ * n <= 2^26. */
+int lulesh_probe_dadd(const double* a, const double* b, double* native, double* ipipe, int64_t n);
 
 #ifdef __cplusplus
 }

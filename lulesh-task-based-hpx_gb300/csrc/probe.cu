@@ -1,7 +1,8 @@
 // Pipe-rate probe (liblulesh_probe.so, not the product library): the double
 // FMA, add, divide and square-root throughput and the float FMA throughput of
 // the current GPU, for the FP64 roof that bounds the double-precision step
-// (the benchmark reports kernel rates against it).
+// (the benchmark reports kernel rates against it), and the rates of the
+// integer-pipe multiply and add the fast kernels use beside the FP64 pipe.
 //
 // Each thread runs 8 independent dependency chains of one operation in a
 // loop; the grid is 8 blocks of 256 threads per SM. Rates are operations per
@@ -11,6 +12,7 @@
 #include "lulesh_gb300.h"
 #include "lulesh_probe.h"
 #include "fp64_emu.cuh"
+#include "fp64_emu_add.cuh"
 
 namespace {
 
@@ -29,6 +31,8 @@ __global__ void k_probe(double* out, int iters, double a, double b) {
             if (OP == 4) r[k] = r[k] * a;                                   // FP64 pipe multiply
             if (OP == 5) r[k] = lulesh::dmul_ipipe(r[k], a);                // integer-pipe multiply
             if (OP == 6) r[k] = (k & 1) ? lulesh::dmul_ipipe(r[k], a) : r[k] * a;  // half each
+            if (OP == 7) r[k] = lulesh::dadd_ipipe(r[k], b);                // integer-pipe add
+            if (OP == 8) r[k] = (k & 1) ? lulesh::dadd_ipipe(r[k], b) : r[k] + b;  // half each
         }
     }
     double s = 0.0;
@@ -52,7 +56,7 @@ __global__ void k_probe_f32(float* out, int iters, float a, float b) {
 
 }  // namespace
 
-extern "C" int lulesh_probe_pipe_rates(double out[8]) {
+extern "C" int lulesh_probe_pipe_rates(double out[10]) {
     if (!out) return LULESH_EINVAL;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return LULESH_ENODEV;
@@ -64,9 +68,9 @@ extern "C" int lulesh_probe_pipe_rates(double out[8]) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int iters[8] = {2000, 2000, 200, 200, 20000, 2000, 2000, 2000};
+    const int iters[10] = {2000, 2000, 200, 200, 20000, 2000, 2000, 2000, 2000, 2000};
     int st = LULESH_OK;
-    for (int op = 0; op < 8 && st == LULESH_OK; ++op) {
+    for (int op = 0; op < 10 && st == LULESH_OK; ++op) {
         float ms = 0.f;
         for (int rep = 0; rep < 2; ++rep) {  // first pass warms up
             cudaEventRecord(e0);
@@ -79,7 +83,9 @@ extern "C" int lulesh_probe_pipe_rates(double out[8]) {
                 case 4: k_probe_f32<<<blocks, threads>>>(static_cast<float*>(buf), iters[op], 0.999999f, 1e-6f); break;
                 case 5: k_probe<4><<<blocks, threads>>>(d, iters[op], 0.999999, 0.0); break;
                 case 6: k_probe<5><<<blocks, threads>>>(d, iters[op], 0.999999, 0.0); break;
-                default: k_probe<6><<<blocks, threads>>>(d, iters[op], 0.999999, 0.0);
+                case 7: k_probe<6><<<blocks, threads>>>(d, iters[op], 0.999999, 0.0); break;
+                case 8: k_probe<7><<<blocks, threads>>>(d, iters[op], 0.999999, 1e-6); break;
+                default: k_probe<8><<<blocks, threads>>>(d, iters[op], 0.999999, 1e-6);
             }
             cudaEventRecord(e1);
             if (cudaEventSynchronize(e1) != cudaSuccess) st = LULESH_ECUDA;

@@ -9,6 +9,7 @@
 #include "float_pair.cuh"
 #include "lulesh_probe.h"
 #include "fp64_emu.cuh"
+#include "fp64_emu_add.cuh"
 
 namespace lulesh {
 namespace probe {
@@ -32,6 +33,7 @@ __global__ void k_math_probe(int fn, const double* __restrict__ in, double* __re
 }
 
 __device__ __noinline__ double dmul_fp64_pipe(double a, double b) { return a * b; }
+__device__ __noinline__ double dadd_fp64_pipe(double a, double b) { return a + b; }
 
 // The FP64 pipe's product and the integer pipes' product of the same operands.
 __global__ void k_dmul_probe(const double* __restrict__ a, const double* __restrict__ b,
@@ -40,6 +42,15 @@ __global__ void k_dmul_probe(const double* __restrict__ a, const double* __restr
     if (i >= n) return;
     native[i] = dmul_fp64_pipe(a[i], b[i]);
     ipipe[i] = dmul_ipipe(a[i], b[i]);
+}
+
+// The FP64 pipe's sum and the integer pipes' sum of the same operands.
+__global__ void k_dadd_probe(const double* __restrict__ a, const double* __restrict__ b,
+                             double* __restrict__ native, double* __restrict__ ipipe, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    native[i] = dadd_fp64_pipe(a[i], b[i]);
+    ipipe[i] = dadd_ipipe(a[i], b[i]);
 }
 
 }  // namespace probe
@@ -68,7 +79,10 @@ extern "C" int lulesh_probe_math(int32_t fn, const double* in, double* out, int6
     return st;
 }
 
-extern "C" int lulesh_probe_dmul(const double* a, const double* b, double* native, double* ipipe, int64_t n) {
+// The pairs (a, b) on the device through probe kernel k (k_dmul_probe or
+// k_dadd_probe): native and integer-pipe results.
+template <class Kernel>
+static int pair_probe(Kernel k, const double* a, const double* b, double* native, double* ipipe, int64_t n) {
     if (!a || !b || !native || !ipipe || n < 1 || n > (int64_t(1) << 26)) return LULESH_EINVAL;
     const size_t bytes = sizeof(double) * size_t(n);
     double* d = nullptr;
@@ -79,7 +93,7 @@ extern "C" int lulesh_probe_dmul(const double* a, const double* b, double* nativ
         st = LULESH_ECUDA;
     if (st == LULESH_OK) {
         const int count = int(n);
-        lulesh::probe::k_dmul_probe<<<(count + 255) / 256, 256>>>(d, d + n, d + 2 * n, d + 3 * n, count);
+        k<<<(count + 255) / 256, 256>>>(d, d + n, d + 2 * n, d + 3 * n, count);
         if (cudaGetLastError() != cudaSuccess ||
             cudaMemcpy(native, d + 2 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
             cudaMemcpy(ipipe, d + 3 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -87,4 +101,12 @@ extern "C" int lulesh_probe_dmul(const double* a, const double* b, double* nativ
     }
     cudaFree(d);
     return st;
+}
+
+extern "C" int lulesh_probe_dadd(const double* a, const double* b, double* native, double* ipipe, int64_t n) {
+    return pair_probe(lulesh::probe::k_dadd_probe, a, b, native, ipipe, n);
+}
+
+extern "C" int lulesh_probe_dmul(const double* a, const double* b, double* native, double* ipipe, int64_t n) {
+    return pair_probe(lulesh::probe::k_dmul_probe, a, b, native, ipipe, n);
 }

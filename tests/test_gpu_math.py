@@ -136,3 +136,48 @@ def test_integer_pipe_multiply_equals_fp64_pipe(lulesh):
     with np.errstate(all="ignore"):
         host = a * b
     assert np.all((host.view(np.uint64) == native.view(np.uint64)) | (np.isnan(host) & np.isnan(native)))
+
+
+def test_integer_pipe_add_is_the_fp64_add(lulesh):
+    """dadd_ipipe, the integer-pipe double add of the measurement probes (no
+    step kernel uses it: it is slower than the FP64 pipe's add), gives the
+    FP64 pipe's bits for every operand pair: seeded random bit
+    patterns over the whole exponent range (normal, subnormal, zero, infinite
+    and NaN operands, both signs), sums that cancel to a few bits, that land
+    on a rounding tie, that stay subnormal or become normal, and that
+    overflow."""
+    rng = np.random.default_rng(11)
+    n = 1 << 22
+    bits = rng.integers(0, 2 ** 63, size=(2, n), dtype=np.int64).astype(np.uint64)
+    bits[:, : n // 2] |= rng.integers(0, 2, size=(2, n // 2), dtype=np.uint64) << np.uint64(63)
+    a, b = bits.view(np.float64)
+    k = n // 5
+    sign = lambda m: rng.choice([-1.0, 1.0], m)  # noqa: E731
+    # the step's range: exponents near 0, both signs
+    a[:k] = np.ldexp(rng.uniform(1.0, 2.0, k), rng.integers(-60, 60, k)) * sign(k)
+    b[:k] = np.ldexp(rng.uniform(1.0, 2.0, k), rng.integers(-60, 60, k)) * sign(k)
+    # near cancellation: b = -a (1 + j 2^(e-52))
+    j = rng.integers(-2 ** 20, 2 ** 20, k).astype(np.float64)
+    with np.errstate(invalid="ignore"):
+        b[k:2 * k] = -a[k:2 * k] * (1.0 + np.ldexp(j, -52 + rng.integers(-3, 4, k)))
+    # ties: b a power of two half an ulp of a, or below
+    a[2 * k:3 * k] = np.ldexp(rng.uniform(1.0, 2.0, k), rng.integers(-100, 100, k)) * sign(k)
+    b[2 * k:3 * k] = np.ldexp(sign(k), np.frexp(a[2 * k:3 * k])[1] - 54 - rng.integers(0, 12, k))
+    # subnormal operands and sums, and sums at the top of the range
+    m = 1 << 16
+    a[3 * k:3 * k + m] = np.ldexp(rng.uniform(-2.0, 2.0, m), -1022 - rng.integers(0, 60, m))
+    b[3 * k:3 * k + m] = np.ldexp(rng.uniform(-2.0, 2.0, m), -1022 - rng.integers(0, 60, m))
+    a[3 * k + m:3 * k + 2 * m] = np.ldexp(rng.uniform(1.0, 2.0, m), 1023) * sign(m)
+    b[3 * k + m:3 * k + 2 * m] = np.ldexp(rng.uniform(1.0, 2.0, m), 1023 - rng.integers(0, 60, m)) * sign(m)
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, -2.2e-308, 1e308, 1e-308, 1.0,
+                        -3.0])
+    sa, sb = np.meshgrid(special, special)
+    a[-sa.size:], b[-sb.size:] = sa.ravel(), sb.ravel()
+    native, ipipe = lulesh.probe_dadd(a, b)
+    same = native.view(np.uint64) == ipipe.view(np.uint64)
+    both_nan = np.isnan(native) & np.isnan(ipipe)
+    assert np.all(same | both_nan), np.flatnonzero(~(same | both_nan))[:8]
+    # and both are the IEEE sums the host computes
+    with np.errstate(all="ignore"):
+        host = a + b
+    assert np.all((host.view(np.uint64) == native.view(np.uint64)) | (np.isnan(host) & np.isnan(native)))

@@ -36,7 +36,7 @@ def test_probes_live_in_their_own_library(lulesh):
     declares."""
     probe_header = ROOT / "lulesh-task-based-hpx_gb300" / "csrc" / "lulesh_probe.h"
     names = declared_functions(probe_header)
-    assert names == ["lulesh_probe_dmul", "lulesh_probe_math", "lulesh_probe_pipe_rates"]
+    assert names == ["lulesh_probe_dadd", "lulesh_probe_dmul", "lulesh_probe_math", "lulesh_probe_pipe_rates"]
     plib = lulesh.probe_library()
     assert all(hasattr(plib, n) for n in names)
     product = C.CDLL(str(lulesh.LIB_PATH))
