@@ -107,8 +107,9 @@ struct lulesh_dev {
     double* stage[3] = {nullptr, nullptr, nullptr};
     // device-side timing (lulesh_dev_profile_begin/end)
     bool profiling = false;
-    cudaEvent_t ev[5] = {};
+    cudaEvent_t ev[2][5] = {};  // per-phase boundaries; two sets, for a cycle and the next one's forces
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    cudaEvent_t ev_done = nullptr;  // a cycle's readback of its dt minima and error word
     double kernel_ms[4] = {0, 0, 0, 0};
     int64_t prof_cycles = 0, prof_launch0 = 0;
 };
@@ -346,33 +347,55 @@ int upload_mesh(const Mesh& m, const lulesh_domain_view* v, int precision, cudaS
     return LULESH_OK;
 }
 
-int run_cycle(lulesh_dev* d, double dt) {
+// A cycle in three parts, so that the host loop can queue the next cycle's
+// force phase, which reads neither dt nor the time, before it waits for the
+// current cycle's dt minima (lulesh_dev_run). `set` picks the profiling
+// events of the cycle (two sets: a cycle's and the next one's forces).
+//
+// The force phase: the error word cleared, the element geometry formed where
+// it is stale, forces.
+int queue_forces(lulesh_dev* d, int set) {
     const Mesh& m = d->m;
     const bool prof = d->profiling;
     CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
     const bool geo = d->L.forces_geo != nullptr;
-    if (prof) CK(cudaEventRecord(d->ev[0], d->stream));
+    if (prof) CK(cudaEventRecord(d->ev[set][0], d->stream));
     if (geo) {
         if (!d->geo_valid) d->launches += d->L.geometry(m, d->stream);
         d->launches += d->L.forces_geo(m, d->stream);
     } else {
         d->launches += d->L.forces(m, d->stream);
     }
-    if (prof) CK(cudaEventRecord(d->ev[1], d->stream));
+    if (prof) CK(cudaEventRecord(d->ev[set][1], d->stream));
+    return LULESH_OK;
+}
+// The rest of the cycle with time step dt, then the readback of its dt
+// minima and error word (event ev_done).
+int queue_rest(lulesh_dev* d, double dt, int set) {
+    const Mesh& m = d->m;
+    const bool prof = d->profiling;
+    const bool geo = d->L.forces_geo != nullptr;
+    if (!d->ev_done) CK(cudaEventCreateWithFlags(&d->ev_done, cudaEventDisableTiming));
     d->launches += d->L.nodes(m, dt, d->stream);
-    if (prof) CK(cudaEventRecord(d->ev[2], d->stream));
+    if (prof) CK(cudaEventRecord(d->ev[set][2], d->stream));
     d->launches += geo ? d->L.kinematics_geo(m, dt, d->stream) : d->L.kinematics(m, dt, d->stream);
     d->geo_valid = geo;
-    if (prof) CK(cudaEventRecord(d->ev[3], d->stream));
+    if (prof) CK(cudaEventRecord(d->ev[set][3], d->stream));
     d->launches += d->L.material(m, d->stream);
-    if (prof) CK(cudaEventRecord(d->ev[4], d->stream));
+    if (prof) CK(cudaEventRecord(d->ev[set][4], d->stream));
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(d->h_result, m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
-    CK(cudaStreamSynchronize(d->stream));
-    if (prof) {
+    CK(cudaEventRecord(d->ev_done, d->stream));
+    return LULESH_OK;
+}
+// Waits for the cycle's readback (not for work queued after it) and returns
+// its status.
+int finish_cycle(lulesh_dev* d, int set) {
+    CK(cudaEventSynchronize(d->ev_done));
+    if (d->profiling) {
         for (int k = 0; k < 4; ++k) {
             float ms = 0.f;
-            CK(cudaEventElapsedTime(&ms, d->ev[k], d->ev[k + 1]));
+            CK(cudaEventElapsedTime(&ms, d->ev[set][k], d->ev[set][k + 1]));
             d->kernel_ms[k] += ms;
         }
         ++d->prof_cycles;
@@ -382,6 +405,12 @@ int run_cycle(lulesh_dev* d, double dt) {
         return d->h_result->err;
     }
     return LULESH_OK;
+}
+
+int run_cycle(lulesh_dev* d, double dt) {
+    int st = queue_forces(d, 0);
+    if (st == LULESH_OK) st = queue_rest(d, dt, 0);
+    return st == LULESH_OK ? finish_cycle(d, 0) : st;
 }
 
 int build_graph(lulesh_dev* d) {
@@ -510,8 +539,10 @@ int lulesh_dev_create_problem(const lulesh_problem* p, int32_t precision, lulesh
 void lulesh_dev_destroy(lulesh_dev* d) {
     if (!d) return;
     if (d->stream) cudaStreamSynchronize(d->stream);
-    for (cudaEvent_t e : d->ev)
-        if (e) cudaEventDestroy(e);
+    for (auto& set : d->ev)
+        for (cudaEvent_t e : set)
+            if (e) cudaEventDestroy(e);
+    if (d->ev_done) cudaEventDestroy(d->ev_done);
     if (d->ev_begin) cudaEventDestroy(d->ev_begin);
     if (d->ev_end) cudaEventDestroy(d->ev_end);
     if (d->graph) cudaGraphExecDestroy(d->graph);
@@ -830,10 +861,27 @@ int lulesh_dev_run(lulesh_dev* d, lulesh_time_state* ts, int32_t max_cycles, int
     if (!d || !ts) return LULESH_EINVAL;
     int32_t n = 0;
     int st = LULESH_OK;
+    // The time loop of hpx_main (lulesh.cc:2374-2386): TimeIncrement on the
+    // host, then the cycle. The loop condition of the next cycle is known
+    // once this cycle's TimeIncrement has run, so when another cycle follows,
+    // its force phase (which reads neither dt nor the time) is queued before
+    // the host waits for this cycle's dt minima: the GPU computes it while
+    // the minima come back and the next TimeIncrement runs. Same operations,
+    // same order on the stream, same results.
+    bool forces_queued = false;
+    int set = 0;
     while (ts->time < ts->stoptime && ts->cycle < max_cycles) {
         lulesh_time_increment(ts);
-        st = lulesh_dev_step(d, ts->deltatime, &ts->dtcourant, &ts->dthydro);
+        if (!forces_queued) st = queue_forces(d, set);
+        if (st == LULESH_OK) st = queue_rest(d, ts->deltatime, set);
         if (st != LULESH_OK) break;
+        forces_queued = ts->time < ts->stoptime && ts->cycle < max_cycles;
+        if (forces_queued) st = queue_forces(d, set ^ 1);
+        if (st == LULESH_OK) st = finish_cycle(d, set);
+        if (st != LULESH_OK) break;  // a queued force phase just runs on scratch arrays
+        ts->dtcourant = d->h_result->dtcourant;
+        ts->dthydro = d->h_result->dthydro;
+        set ^= 1;
         ++n;
     }
     if (cycles_run) *cycles_run = n;
@@ -964,7 +1012,8 @@ int lulesh_dev_gradients(lulesh_dev* d, double* out6) {
 int lulesh_dev_profile_begin(lulesh_dev* d) {
     if (!d) return LULESH_EINVAL;
     if (!d->ev_begin) {
-        for (cudaEvent_t& e : d->ev) CK(cudaEventCreate(&e));
+        for (auto& set : d->ev)
+            for (cudaEvent_t& e : set) CK(cudaEventCreate(&e));
         CK(cudaEventCreate(&d->ev_begin));
         CK(cudaEventCreate(&d->ev_end));
     }
