@@ -209,8 +209,12 @@ int lulesh_leapfrog(lulesh_dev* dev, lulesh_domain_view* host);
 
 /* The time loop of hpx_main (lulesh.cc:2374-2386) on device-resident state:
  * while (time < stoptime && cycle < max_cycles) { TimeIncrement; step }.
- * TimeIncrement runs on the host between cycles. *cycles_run counts the
- * cycles this call ran. */
+ * TimeIncrement runs on the host between cycles; while it waits for a
+ * cycle's dt minima, the next cycle's force phase (which reads neither dt
+ * nor the time) is already queued when another cycle follows. *cycles_run
+ * counts the cycles this call ran. On LULESH_EVOLUME that queued force phase
+ * may still run on the handle's stream after the call returns; it writes
+ * only scratch arrays, and later calls on the handle wait for it. */
 int lulesh_dev_run(lulesh_dev* dev, lulesh_time_state* ts, int32_t max_cycles, int32_t* cycles_run);
 
 /* The same time loop with TimeIncrement on the device and each cycle's

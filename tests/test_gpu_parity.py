@@ -215,6 +215,66 @@ def test_graph_loop_equals_host_loop(lulesh, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp64_exact", "mixed"])
+def test_host_loop_equals_single_steps(lulesh, precision):
+    """lulesh_dev_run queues each next cycle's force phase before it waits for
+    the current cycle's dt minima. Its results equal single lulesh_dev_step
+    calls with the host TimeIncrement between them, bit for bit, when the
+    loop stops at a cycle cap and then runs on to the stoptime."""
+    a, b = lulesh.HostDomain(9), lulesh.HostDomain(9)
+    dev_a, dev_b = lulesh.Device(a, precision), lulesh.Device(b, precision)
+    assert dev_a.run(37) == 37
+    n = dev_a.run()  # on to the stoptime
+    ts = b.time_state
+    m = 0
+    while ts.time < ts.stoptime:
+        b.time_increment()
+        ts.dtcourant, ts.dthydro = dev_b.step(ts.deltatime)
+        m += 1
+    assert 37 + n == m == a.cycle == b.cycle
+    dev_a.download()
+    dev_b.download()
+    for f in ("time", "deltatime", "dtcourant", "dthydro"):
+        assert getattr(a.time_state, f) == getattr(b.time_state, f), f
+    for f in NODE + ELEM:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    dev_a.close()
+    dev_b.close()
+
+
+def test_host_loop_error_with_next_forces_queued(lulesh):
+    """A cycle of lulesh_dev_run that raises VolumeError has the next cycle's
+    force phase already queued behind it. The loop reports the failing
+    cycle's error and element; the handle stays usable: with the state of a
+    good run uploaded, it runs on bit for bit like that run."""
+    dom = lulesh.HostDomain(6)
+    dev = lulesh.Device(dom, "fp64")
+    assert dev.run(3) == 3
+    dev.download()
+    dom.v[40] = -0.5
+    dev.upload(lulesh.F_V)
+    with pytest.raises(lulesh.LuleshError) as ei:
+        dev.run(10)
+    assert ei.value.status == lulesh.EVOLUME
+    assert dev.error_elem == 40
+    good = lulesh.HostDomain(6)
+    good_dev = lulesh.Device(good, "fp64")
+    assert good_dev.run(3) == 3
+    good_dev.download()
+    for f in NODE + ELEM:
+        getattr(dom, f)[:] = getattr(good, f)
+    for f in ("time", "deltatime", "dtcourant", "dthydro", "cycle"):
+        setattr(dom.time_state, f, getattr(good.time_state, f))
+    dev.upload()
+    assert dev.run(12) == good_dev.run(12) == 9
+    dev.download()
+    good_dev.download()
+    for f in NODE + ELEM:
+        np.testing.assert_array_equal(getattr(dom, f), getattr(good, f), err_msg=f)
+    dev.close()
+    good_dev.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_exact", "mixed"])
 def test_run_to_run_determinism(lulesh, precision):
     a, _, _ = _run_device(lulesh, 11, 21, 1, 1, precision, its=120)
     b, _, _ = _run_device(lulesh, 11, 21, 1, 1, precision, its=120)
