@@ -10,7 +10,7 @@
  *    LULESH_OK or a negative code; LULESH_EVOLUME is the reference's
  *    VolumeError (lulesh.h:30), the condition on which the reference calls
  *    exit(VolumeError) (lulesh.cc:821, 908, 1262).
- *  - A lulesh_dev handle owns one CUDA stream (lulesh_leapfrog creates four
+ *  - A lulesh_dev handle owns one CUDA stream (lulesh_leapfrog creates five
  *    more on its first call) and device copies of every Domain array the
  *    step touches. Use a handle from one host thread at a
  *    time. Host arrays stay owned by the caller.

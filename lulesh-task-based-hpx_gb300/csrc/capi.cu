@@ -92,7 +92,8 @@ struct lulesh_dev {
     cudaStream_t mstream = nullptr;  // downloads of the compute stream's results
     cudaStream_t stream2 = nullptr;  // second compute stream: every other slab
     cudaStream_t mstream2 = nullptr; // downloads of the second compute stream's results
-    cudaEvent_t ev_up = nullptr, ev_e = nullptr, ev_s2 = nullptr, ev_join = nullptr;
+    cudaStream_t nstream = nullptr;  // the node ranges, beside the force slabs
+    cudaEvent_t ev_up = nullptr, ev_e = nullptr, ev_s2 = nullptr, ev_join = nullptr, ev_s1 = nullptr;
     // one per slab: upload, mirror (mixed), node range, kinematics and material done
     std::vector<cudaEvent_t> ev_slab, ev_mir, ev_node, ev_kin, ev_mat;
     int32_t* upload_flag = nullptr;  // [kLeapfrogSlabs] per-slab "host changed a coordinate" (arena)
@@ -551,11 +552,11 @@ void lulesh_dev_destroy(lulesh_dev* d) {
     if (d->h_time) cudaFreeHost(d->h_time);
     if (d->h_verify) cudaFreeHost(d->h_verify);
     if (d->cstream) cudaStreamSynchronize(d->cstream);
-    for (cudaEvent_t e : {d->ev_up, d->ev_e, d->ev_s2, d->ev_join})
+    for (cudaEvent_t e : {d->ev_up, d->ev_e, d->ev_s2, d->ev_join, d->ev_s1})
         if (e) cudaEventDestroy(e);
     for (auto* evs : {&d->ev_slab, &d->ev_mir, &d->ev_node, &d->ev_kin, &d->ev_mat})
         for (cudaEvent_t e : *evs) cudaEventDestroy(e);
-    for (cudaStream_t st : {d->stream2, d->mstream2}) {
+    for (cudaStream_t st : {d->stream2, d->mstream2, d->nstream}) {
         if (!st) continue;
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
@@ -643,16 +644,18 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
         CK(cudaStreamCreateWithFlags(&d->mstream, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&d->stream2, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&d->mstream2, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&d->ev_up, &d->ev_e, &d->ev_s2, &d->ev_join})
+        CK(cudaStreamCreateWithFlags(&d->nstream, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&d->ev_up, &d->ev_e, &d->ev_s2, &d->ev_join, &d->ev_s1})
             CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
     const Mesh& m = d->m;
     const double dt = v->time->deltatime;
     // The cycle runs in slabs of whole element planes (the handle's matOrder
-    // is slab-major), on five streams: uploads (cstream), compute (stream,
+    // is slab-major), on six streams: uploads (cstream), compute (stream,
     // and stream2 for every other slab, so that the tail of one slab's
-    // launch overlaps the next) and downloads (mstream for the results of
-    // stream, mstream2 for those of stream2, so that each goes down as soon
+    // launch overlaps the next; nstream for the node ranges, beside the
+    // force slabs) and downloads (mstream for the results of stream and
+    // nstream, mstream2 for those of stream2, so that each goes down as soon
     // as it is ready).
     // The host<->device link (about 190 GB/s each way on GB300's C2C,
     // against 930 MB a cycle at s=150) paces the call as much as the GPU
@@ -662,8 +665,9 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     //     -> forces of slab k;
     //   node update in ranges, one after every two force slabs (the node
     //     planes below the next slab's, whose corner forces are then all
-    //     formed) and the rest after the last, each range's fields going
-    //     down behind it during the force phase;
+    //     formed; later slabs' uploads, checks and forces touch only node
+    //     planes above them, so the ranges run beside the force phase) and
+    //     the rest after the last, each range's fields going down behind it;
     //   kinematics in slabs of two force slabs, each one's fields going down
     //     while the next runs, so that they are down before the material
     //     phase's fields are ready;
@@ -717,12 +721,14 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
         return LULESH_OK;
     };
 
-    // Node update of nodes [a, b) on the compute stream after both compute
+    // Node update of nodes [a, b) on the node stream after both compute
     // streams' work so far, then those node fields go down. With the
     // geometry form the positions advanced are the uploaded copies.
     auto node_range = [&](int64_t a, int64_t b, cudaEvent_t ev) -> int {
+        CK(cudaEventRecord(d->ev_s1, d->stream));
         CK(cudaEventRecord(d->ev_s2, d->stream2));
-        CK(cudaStreamWaitEvent(d->stream, d->ev_s2, 0));
+        CK(cudaStreamWaitEvent(d->nstream, d->ev_s1, 0));
+        CK(cudaStreamWaitEvent(d->nstream, d->ev_s2, 0));
         Mesh mn = m;  // nodes [a, b) as a mesh of b - a nodes at offset a
         mn.numNode = int(b - a);
         for (double** f : {&mn.x, &mn.y, &mn.z, &mn.xd, &mn.yd, &mn.zd, &mn.xdd, &mn.ydd, &mn.zdd, &mn.fx,
@@ -735,9 +741,9 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
         if (mn.pxp)
             for (float2** f : {&mn.pxp, &mn.pyp, &mn.pzp, &mn.vxp, &mn.vyp, &mn.vzp}) *f += a;
         d->launches += geo ? lulesh::fp64::launch_nodes_upload(mn, dt, d->stage[0] + a, d->stage[1] + a,
-                                                               d->stage[2] + a, d->stream)
-                           : d->L.nodes(mn, dt, d->stream);
-        CK(cudaEventRecord(ev, d->stream));
+                                                               d->stage[2] + a, d->nstream)
+                           : d->L.nodes(mn, dt, d->nstream);
+        CK(cudaEventRecord(ev, d->nstream));
         CK(cudaStreamWaitEvent(d->mstream, ev, 0));
         for (const Copy& c : out_nodes)
             CK(cudaMemcpyAsync(static_cast<double*>(const_cast<void*>(c.host)) + a,
@@ -804,6 +810,8 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     if (e_in) CK(cudaMemcpyAsync(e_in->dev, e_in->host, e_in->bytes, cudaMemcpyHostToDevice, d->cstream));
     CK(cudaEventRecord(d->ev_e, d->cstream));
     if (int st = node_range(node_next, m.numNode, d->ev_node[nranges])) return st;
+    // the kinematics read every node: both compute streams wait for the last range
+    CK(cudaStreamWaitEvent(d->stream, d->ev_node[nranges], 0));
     CK(cudaStreamWaitEvent(d->stream2, d->ev_node[nranges], 0));
     for (int k = 0; k < slabs; k += 2) {
         const int64_t e0 = e_lo[k], e1 = e_hi[std::min(k + 1, slabs - 1)];
