@@ -45,14 +45,24 @@ def build(ref: bool | None = None) -> None:
     """Builds the port (always) and the reference binary (when its sources
     exist). Where the checkout exists, its sources are also installed into
     baseline/_ref, so that a machine without it (the GPU host) can build and
-    time the reference's own code."""
+    time the reference's own code. With ref=None (build it where the sources
+    are) a failed reference build only prints a message: the binary is an
+    optional checker and baseline; ref=True makes it an error."""
     subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
+    required = ref is True
     if ref is None:
         ref = REF_SOURCES.is_dir()
-    if ref:
-        subprocess.run(["make", "-s", "-j2", "-C", str(HERE), "ref", f"REF_DIR={REF_SOURCES}"], check=True)
-        if REF_SOURCES.resolve() != REF_INSTALLED.resolve():
-            subprocess.run(["make", "-s", "-C", str(HERE), "install-ref"], check=True)
+    if not ref:
+        return
+    r = subprocess.run(["make", "-s", "-j2", "-C", str(HERE), "ref", f"REF_DIR={REF_SOURCES}"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        if required:
+            raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")
+        print(f"oracle: the reference binary was not built ({REF_SOURCES}): {r.stderr.strip()[-300:]}")
+        return
+    if REF_SOURCES.resolve() != REF_INSTALLED.resolve():
+        subprocess.run(["make", "-s", "-C", str(HERE), "install-ref"], check=True)
 
 
 _lib = None
