@@ -437,13 +437,17 @@ def run_ours(args) -> None:
     barrier(world)
     sync()
     t0 = time.perf_counter()
+    call_ms = []
     for _ in range(K):
+        t1 = time.perf_counter()
         dom.time_increment()
         dev.leapfrog()
+        call_ms.append(1e3 * (time.perf_counter() - t1))
     sync()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     barrier(world)
     e2e_value = world * ne * K / e2e_s
+    call_ms.sort()
     h2d = (6 * nn + 5 * ne) * 8
     d2h = (12 * nn + 11 * ne) * 8 + 16
     link = link_rates(local)
@@ -547,6 +551,10 @@ def run_ours(args) -> None:
                 "how": "lulesh_leapfrog per cycle: upload step inputs from pinned host arrays, "
                        "run, download every field the step writes; wall clock",
                 "ms_per_step": round(1e3 * e2e_s / K, 4),
+                "call_ms": {"min": round(call_ms[0], 3), "median": round(call_ms[len(call_ms) // 2], 3),
+                            "max": round(call_ms[-1], 3),
+                            "note": "wall time of each timed call (value uses the whole window); the host "
+                                    "side of this figure has varied between boxes"},
                 "link_gbs": link,
                 "link_floor_ms": round(1e3 * d2h / (link["d2h"] * 1e9), 3),
                 "link_floor_note": "the step's downloads alone at the measured device-to-host rate"},
