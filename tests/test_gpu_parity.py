@@ -283,13 +283,14 @@ def test_run_to_run_determinism(lulesh, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp64_exact", "mixed"])
-@pytest.mark.parametrize("size", [1, 3, 5, 10, 19])
+@pytest.mark.parametrize("size", [1, 3, 5, 10, 19, 33])
 def test_leapfrog_on_host_buffers_equals_resident_run(lulesh, precision, size):
     """lulesh_leapfrog (upload, step, download each cycle, the literal
     drop-in for LagrangeLeapFrog(Domain&), run slab by slab with its copies
     overlapping the cycle) gives the device-resident bits, dt constraints
     included: one slab (s=1), fewer slabs than 8 with an odd count (s=3, 5:
-    a kinematics group of one slab), 8 slabs of uneven thickness (s=10, 19)."""
+    a kinematics group of one slab), 8 slabs of uneven thickness (s=10, 19,
+    33)."""
     # the resident run first: 25 cycles, or fewer where the stoptime comes
     # first (s=1 reaches it in 1 cycle, s=3 in 23)
     b, _, n = _run_device(lulesh, size, 11, 1, 1, precision, its=25)
@@ -309,13 +310,17 @@ def test_leapfrog_on_host_buffers_equals_resident_run(lulesh, precision, size):
 # s=10 runs the drop-in call in 8 slabs of element planes [0,1) [1,2) [2,3)
 # [3,5) [5,6) [6,7) [7,8) [8,10); moved nodes: plane 1 (row 1, column 5), the
 # slab boundary plane 5, and the top plane 10 (in the last node range).
-@pytest.mark.parametrize("node", [137, 5 * 121 + 5 * 11 + 5, 10 * 121 + 5 * 11 + 3])
-def test_leapfrog_with_host_changed_coordinates(lulesh, node):
+# s=33 (slabs of 4 and 5 planes): nodes in plane 1, plane 32 and the top
+# plane 33.
+@pytest.mark.parametrize("size,node", [(10, 137), (10, 5 * 121 + 5 * 11 + 5), (10, 10 * 121 + 5 * 11 + 3),
+                                       (33, 1156 + 5 * 34 + 5), (33, 32 * 1156 + 5 * 34 + 5),
+                                       (33, 33 * 1156 + 5 * 34 + 3)])
+def test_leapfrog_with_host_changed_coordinates(lulesh, size, node):
     """lulesh_leapfrog reuses the element geometry its previous step stored
     only for slabs whose nodes the host left as that step made them. With
     one node moved on the host between two calls, the drop-in run stays bit
     for bit the device-resident run given the same move by upload."""
-    a, b = lulesh.HostDomain(10), lulesh.HostDomain(10)
+    a, b = lulesh.HostDomain(size), lulesh.HostDomain(size)
     dev_a, dev_b = lulesh.Device(a, "fp64"), lulesh.Device(b, "fp64")
     for cycle in range(12):
         if cycle == 6:
