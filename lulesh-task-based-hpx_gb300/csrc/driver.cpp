@@ -54,7 +54,7 @@ int main(int argc, char** argv) {
         if (a == "--q") { quiet = 1; continue; }
         if (a == "--p") { prog = 1; continue; }
         if (a == "--v") {
-            std::printf("Use of --v requires a build with viz output (Silo), which this build does not have\n");
+            std::printf("Use of --v requires a build with viz output (Silo); lulesh-gb300 has none\n");
             return -1;
         }
         if (a == "--graph") { graph = 1; continue; }
