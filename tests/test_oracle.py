@@ -105,3 +105,17 @@ def test_energy_scale_changes_only_the_deposit(oracle_mod):
     assert b.field("e")[0] == a.field("e")[0] * 1.7
     assert b.scalar("deltatime") < a.scalar("deltatime")
     np.testing.assert_array_equal(a.field("x"), b.field("x"))
+
+
+@pytest.mark.skipif(not (oracle.REF_SOURCES / "lulesh.cc").exists()
+                    or oracle.REF_SOURCES.resolve() == oracle.REF_INSTALLED.resolve(),
+                    reason="the reference checkout is not on this machine")
+def test_installed_reference_is_the_unmodified_sources(oracle_mod):
+    """make install-ref copies the reference's sources into baseline/_ref
+    (where a machine without the checkout builds and times them) byte for
+    byte, and nothing else."""
+    subprocess.run(["make", "-s", "-C", str(oracle_mod.HERE), "install-ref"], check=True)
+    files = ("lulesh.cc", "lulesh.h", "lulesh-init.cc", "lulesh-util.cc", "lulesh-viz.cc", "LICENSE")
+    assert sorted(p.name for p in oracle_mod.REF_INSTALLED.iterdir()) == sorted(files)
+    for f in files:
+        assert (oracle_mod.REF_INSTALLED / f).read_bytes() == (oracle_mod.REF_SOURCES / f).read_bytes(), f
