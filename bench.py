@@ -395,7 +395,7 @@ def reference_code_rate(s: int, r: int, cycles: int) -> dict | None:
     kv = dict(x.split("=", 1) for x in line.split()[1:])
     elapsed = float(kv["elapsed"])
     return {"value": round(s ** 3 * cycles / elapsed, 1), "unit": UNIT, "threads": 1,
-            "sample": f"{cycles} cycles of s={s} r={r} ({elapsed:.1f} s by the reference's own timer)",
+            "sample": f"{cycles} cycles of s={s} r={r} ({elapsed:.3f} s by the reference's own timer)",
             "code": "the reference's unmodified sources with the sequential HPX stand-in, built on this "
                     "host (-O3 -ffp-contract=off)"}
 

@@ -155,3 +155,22 @@ def test_gpus_flag_must_match_world_size():
                        env={k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK")})
     assert r.returncode != 0
     assert "WORLD_SIZE is 1" in r.stderr
+
+
+def test_reference_code_rate_reads_the_reference_timer():
+    """bench.reference_code_rate runs the reference's own binary (its
+    unmodified sources, built where they are) and takes the elapsed time the
+    reference prints for its time loop: one thread, elements x cycles / that
+    time."""
+    sys.path.insert(0, str(ROOT))
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import bench
+    import oracle
+
+    if not (oracle.REF_SOURCES / "lulesh.cc").exists():
+        pytest.skip("the reference sources are not on this machine")
+    r = bench.reference_code_rate(24, 11, 6)
+    assert r is not None and r["threads"] == 1 and r["unit"] == bench.UNIT
+    elapsed = float(r["sample"].split("(")[1].split(" s")[0])
+    assert elapsed > 0
+    assert r["value"] == pytest.approx(24 ** 3 * 6 / elapsed, rel=0.05)
