@@ -743,6 +743,45 @@ def run_reference(args) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_timeline(args) -> None:
+    """--timeline: the drop-in call's stage timeline at --size (double and
+    mixed), from CUDA events on the streams that do the work; after 3
+    resident and 3 drop-in warm-up cycles, the last of --steps timed calls.
+    Prints one JSON line: per stage kind its first and last mark (ms after
+    the call's first device work), the marks themselves, the call's wall
+    time."""
+    lul = load_package()
+    lul.set_device(0)
+    out = {"workload": workload(args.size, args.regions), "timeline": {}}
+    for prec in ("fp64", "mixed"):
+        dom = lul.HostDomain(args.size, args.regions, 1, 1)
+        dev = lul.Device(dom, prec)
+        dev.run(dom.cycle + 3)
+        dev.download()
+        dom.pin(True)
+        for _ in range(3):
+            dom.time_increment()
+            dev.leapfrog()
+        dev.timeline(True)
+        walls = []
+        for _ in range(max(args.steps, 1)):
+            dom.time_increment()
+            dev.leapfrog()
+            walls.append(dev.timeline_read()["wall_ms"])
+        t = dev.timeline_read()
+        stages = {}
+        for name, _, ms in t["marks"]:
+            lo, hi = stages.get(name, (ms, ms))
+            stages[name] = (min(lo, ms), max(hi, ms))
+        out["timeline"][prec] = {
+            "stages_first_last_ms": {k: [round(a, 3), round(b, 3)] for k, (a, b) in stages.items()},
+            "marks": [[n, i, round(ms, 3)] for n, i, ms in t["marks"]],
+            "wall_ms_last": round(t["wall_ms"], 3), "wall_ms_median": round(sorted(walls)[len(walls) // 2], 3)}
+        dev.close()
+        dom.close()
+    print(json.dumps(out), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -760,6 +799,8 @@ def main() -> None:
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--batch-problems", type=int, default=64)
     ap.add_argument("--batch-seed", type=int, default=2024)
+    ap.add_argument("--timeline", action="store_true",
+                    help="print the drop-in call's stage timeline (double and mixed) instead")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -771,7 +812,9 @@ def main() -> None:
 
     if not oracle.LIB_PATH.exists():
         oracle.build(ref=False)
-    if args.impl == "reference":
+    if args.timeline:
+        run_timeline(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -362,6 +362,34 @@ typedef struct lulesh_profile {
 int lulesh_dev_profile_begin(lulesh_dev* dev);
 int lulesh_dev_profile_end(lulesh_dev* dev, lulesh_profile* out);
 
+/* Stage timeline of lulesh_leapfrog (no counterpart in the reference). With
+ * the timeline on, each call records a CUDA event, on the stream that does
+ * the work, at every stage boundary of its slab pipeline;
+ * lulesh_leapfrog_timeline_read returns the last call's marks: ms[k] is the
+ * time of mark k after the call's first device work, stage[k] its kind
+ * (LULESH_TL_*), index[k] its slab, node range or kinematics group, and
+ * wall_ms the call's wall time on the host. Off (the default) it costs
+ * nothing. */
+#define LULESH_TL_UPLOAD 1     /* a slab's inputs are on the device */
+#define LULESH_TL_FORCES 2     /* a slab's corner forces are formed */
+#define LULESH_TL_ENERGY_UP 3  /* the energy is on the device */
+#define LULESH_TL_NODES 4      /* a node range is updated */
+#define LULESH_TL_NODES_DOWN 5 /* its node fields are in host memory */
+#define LULESH_TL_KIN 6        /* a kinematics group is done */
+#define LULESH_TL_KIN_DOWN 7   /* its element fields are in host memory */
+#define LULESH_TL_MAT 8        /* a material slab is done */
+#define LULESH_TL_MAT_DOWN 9   /* its element fields are in host memory */
+#define LULESH_TL_END 10       /* the dt minima and error word are back */
+#define LULESH_TL_MAX 96
+typedef struct lulesh_timeline {
+    int32_t n;
+    int32_t stage[LULESH_TL_MAX], index[LULESH_TL_MAX];
+    float ms[LULESH_TL_MAX];
+    double wall_ms;
+} lulesh_timeline;
+int lulesh_leapfrog_timeline(lulesh_dev* dev, int32_t on);
+int lulesh_leapfrog_timeline_read(const lulesh_dev* dev, lulesh_timeline* out);
+
 /* Courant and hydro time-step constraints without allocating device memory.
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc, such as a host framework that owns every device allocation

@@ -66,6 +66,16 @@ class Profile(C.Structure):
 
 KERNELS = ("forces", "nodes", "kinematics", "material")
 
+TL_MAX = 96
+# stage kinds of lulesh_leapfrog's timeline (LULESH_TL_*)
+TL_STAGES = {1: "upload", 2: "forces", 3: "energy_up", 4: "nodes", 5: "nodes_down", 6: "kinematics",
+             7: "kinematics_down", 8: "material", 9: "material_down", 10: "end"}
+
+
+class Timeline(C.Structure):
+    _fields_ = [("n", C.c_int32), ("stage", C.c_int32 * TL_MAX), ("index", C.c_int32 * TL_MAX),
+                ("ms", C.c_float * TL_MAX), ("wall_ms", C.c_double)]
+
 
 class Problem(C.Structure):
     _fields_ = [("s", C.c_int32), ("nr", C.c_int32), ("balance", C.c_int32), ("cost", C.c_int32),
@@ -160,6 +170,8 @@ def library() -> C.CDLL:
         "lulesh_dev_launch_count": (i64, [vp]),
         "lulesh_dev_profile_begin": (i32, [vp]),
         "lulesh_dev_profile_end": (i32, [vp, C.POINTER(Profile)]),
+        "lulesh_leapfrog_timeline": (i32, [vp, i32]),
+        "lulesh_leapfrog_timeline_read": (i32, [vp, C.POINTER(Timeline)]),
         "lulesh_domain_pin": (i32, [vp, i32]),
         "lulesh_set_device": (i32, [i32]),
         "lulesh_batch_create": (i32, [i32, C.c_uint64, i32, C.POINTER(vp)]),
@@ -382,6 +394,18 @@ class Device:
         _check(self._lib.lulesh_dev_profile_end(self._h, C.byref(p)), "lulesh_dev_profile_end")
         return {"total_ms": p.total_ms, "kernel_ms": dict(zip(KERNELS, list(p.kernel_ms))),
                 "cycles": p.cycles, "launches": p.launches}
+
+    def timeline(self, on: bool = True) -> None:
+        """Records the stage boundaries of the following leapfrog calls."""
+        _check(self._lib.lulesh_leapfrog_timeline(self._h, 1 if on else 0), "lulesh_leapfrog_timeline")
+
+    def timeline_read(self) -> dict:
+        """The last leapfrog call's stage marks: [(stage, index, ms after the
+        call's first device work)] and the call's host wall time."""
+        t = Timeline()
+        _check(self._lib.lulesh_leapfrog_timeline_read(self._h, C.byref(t)), "lulesh_leapfrog_timeline_read")
+        marks = [(TL_STAGES.get(t.stage[k], str(t.stage[k])), t.index[k], t.ms[k]) for k in range(t.n)]
+        return {"marks": marks, "wall_ms": t.wall_ms}
 
     @property
     def error_elem(self) -> int:

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdint>
 #include <cstring>
 #include <new>
@@ -96,6 +97,12 @@ struct lulesh_dev {
     cudaEvent_t ev_up = nullptr, ev_e = nullptr, ev_s2 = nullptr, ev_join = nullptr, ev_s1 = nullptr;
     // one per slab: upload, mirror (mixed), node range, kinematics and material done
     std::vector<cudaEvent_t> ev_slab, ev_mir, ev_node, ev_kin, ev_mat;
+    // lulesh_leapfrog's stage timeline (lulesh_leapfrog_timeline): mark 0 is
+    // the call's first device work, marks 1.. the stage boundaries
+    bool tl_on = false;
+    cudaEvent_t tl_ev[LULESH_TL_MAX + 1] = {};
+    int tl_n = 0;
+    lulesh_timeline tl_last{};
     int32_t* upload_flag = nullptr;  // [kLeapfrogSlabs] per-slab "host changed a coordinate" (arena)
     StepResult* slab_result = nullptr;  // [kLeapfrogSlabs] per material slab: dt minima and block counter
     int32_t* matOrderSlab = nullptr;           // [N_e] slab-major material order (arena)
@@ -544,6 +551,8 @@ void lulesh_dev_destroy(lulesh_dev* d) {
         for (cudaEvent_t e : set)
             if (e) cudaEventDestroy(e);
     if (d->ev_done) cudaEventDestroy(d->ev_done);
+    for (cudaEvent_t e : d->tl_ev)
+        if (e) cudaEventDestroy(e);
     if (d->ev_begin) cudaEventDestroy(d->ev_begin);
     if (d->ev_end) cudaEventDestroy(d->ev_end);
     if (d->graph) cudaGraphExecDestroy(d->graph);
@@ -699,6 +708,18 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     CK(cudaMemsetAsync(&m.result->err, 0, 3 * sizeof(int32_t), d->stream));
     if (have_geo) CK(cudaMemsetAsync(d->upload_flag, 0, sizeof(int32_t) * slabs, d->stream));
     CK(cudaMemsetAsync(d->slab_result, 0, sizeof(StepResult) * slabs, d->stream));
+    const auto t_call = std::chrono::steady_clock::now();
+    d->tl_n = 0;
+    if (d->tl_on) CK(cudaEventRecord(d->tl_ev[0], d->stream));
+    // a stage boundary of the timeline, on the stream that did the work
+    auto mark = [&](int stage, int index, cudaStream_t st) -> int {
+        if (!d->tl_on || d->tl_n >= LULESH_TL_MAX) return LULESH_OK;
+        CK(cudaEventRecord(d->tl_ev[1 + d->tl_n], st));
+        d->tl_last.stage[d->tl_n] = stage;
+        d->tl_last.index[d->tl_n] = index;
+        ++d->tl_n;
+        return LULESH_OK;
+    };
     // the copy streams start after the previous cycle's work on the compute stream
     CK(cudaEventRecord(d->ev_up, d->stream));
     CK(cudaStreamWaitEvent(d->cstream, d->ev_up, 0));
@@ -708,23 +729,25 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
 
     // Element fields [e0, e1) in `out` go down once the work queued so far on
     // compute stream st is done (event ev), on st's download stream.
+    // (stage and index: the timeline's marks of the work and of its download)
     auto elem_down = [&](const std::vector<Copy>& out, int64_t e0, int64_t e1, cudaEvent_t ev,
-                         cudaStream_t st) -> int {
+                         cudaStream_t st, int stage, int index) -> int {
         cudaStream_t down = st == d->stream2 ? d->mstream2 : d->mstream;
         CK(cudaEventRecord(ev, st));
+        if (int r = mark(stage, index, st)) return r;
         CK(cudaStreamWaitEvent(down, ev, 0));
         const size_t off = size_t(e0), cnt = size_t(e1 - e0);
         for (const Copy& c : out)
             CK(cudaMemcpyAsync(static_cast<double*>(const_cast<void*>(c.host)) + off,
                                static_cast<const double*>(c.dev) + off, sizeof(double) * cnt,
                                cudaMemcpyDeviceToHost, down));
-        return LULESH_OK;
+        return mark(stage + 1, index, down);
     };
 
     // Node update of nodes [a, b) on the node stream after both compute
     // streams' work so far, then those node fields go down. With the
     // geometry form the positions advanced are the uploaded copies.
-    auto node_range = [&](int64_t a, int64_t b, cudaEvent_t ev) -> int {
+    auto node_range = [&](int64_t a, int64_t b, cudaEvent_t ev, int r) -> int {
         CK(cudaEventRecord(d->ev_s1, d->stream));
         CK(cudaEventRecord(d->ev_s2, d->stream2));
         CK(cudaStreamWaitEvent(d->nstream, d->ev_s1, 0));
@@ -744,12 +767,13 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
                                                                d->stage[2] + a, d->nstream)
                            : d->L.nodes(mn, dt, d->nstream);
         CK(cudaEventRecord(ev, d->nstream));
+        if (int st = mark(LULESH_TL_NODES, r, d->nstream)) return st;
         CK(cudaStreamWaitEvent(d->mstream, ev, 0));
         for (const Copy& c : out_nodes)
             CK(cudaMemcpyAsync(static_cast<double*>(const_cast<void*>(c.host)) + a,
                                static_cast<const double*>(c.dev) + a, sizeof(double) * size_t(b - a),
                                cudaMemcpyDeviceToHost, d->mstream));
-        return LULESH_OK;
+        return mark(LULESH_TL_NODES_DOWN, r, d->mstream);
     };
     int64_t node_next = 0;  // first node not yet updated
     int nranges = 0;
@@ -758,7 +782,8 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     int64_t node_done = 0;
     for (int sl = 0; sl < slabs; ++sl) {
         if (cube && sl > 0 && (sl & 1) == 0) {  // the node planes below slab sl's
-            if (int st = node_range(node_next, n_lo[sl], d->ev_node[nranges++])) return st;
+            if (int st = node_range(node_next, n_lo[sl], d->ev_node[nranges], nranges)) return st;
+            ++nranges;
             node_next = n_lo[sl];
         }
         const int64_t e0 = e_lo[sl], e1 = e_hi[sl], n1 = n_hi[sl];
@@ -780,6 +805,7 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
                                    cudaMemcpyHostToDevice, d->cstream));
         }
         CK(cudaEventRecord(d->ev_slab[sl], d->cstream));
+        if (int st = mark(LULESH_TL_UPLOAD, sl, d->cstream)) return st;
         cudaStream_t cs = (sl & 1) ? d->stream2 : d->stream;
         CK(cudaStreamWaitEvent(cs, d->ev_slab[sl], 0));
         if (d->precision == LULESH_MIXED) {
@@ -804,12 +830,14 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
         } else {
             d->launches += d->L.forces_range(m, int(e0), int(e1), cs);
         }
+        if (int st = mark(LULESH_TL_FORCES, sl, cs)) return st;
         node_done = n1;
     }
 
     if (e_in) CK(cudaMemcpyAsync(e_in->dev, e_in->host, e_in->bytes, cudaMemcpyHostToDevice, d->cstream));
     CK(cudaEventRecord(d->ev_e, d->cstream));
-    if (int st = node_range(node_next, m.numNode, d->ev_node[nranges])) return st;
+    if (int st = mark(LULESH_TL_ENERGY_UP, 0, d->cstream)) return st;
+    if (int st = node_range(node_next, m.numNode, d->ev_node[nranges], nranges)) return st;
     // the kinematics read every node: both compute streams wait for the last range
     CK(cudaStreamWaitEvent(d->stream, d->ev_node[nranges], 0));
     CK(cudaStreamWaitEvent(d->stream2, d->ev_node[nranges], 0));
@@ -818,7 +846,7 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
         cudaStream_t cs = (k & 2) ? d->stream2 : d->stream;
         d->launches += geo ? d->L.kinematics_geo_range(m, dt, int(e0), int(e1), cs)
                            : d->L.kinematics_range(m, dt, int(e0), int(e1), cs);
-        if (int st = elem_down(out_kin, e0, e1, d->ev_kin[k], cs)) return st;
+        if (int st = elem_down(out_kin, e0, e1, d->ev_kin[k], cs, LULESH_TL_KIN, k / 2)) return st;
     }
     // the material phase reads the kinematics of both compute streams (the
     // Q limiter reads neighbouring elements' gradients) and the energy
@@ -840,7 +868,7 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
         ms.result = d->slab_result + sl;
         part += ms.matGrid;
         d->launches += d->L.material_range(ms, int(e_lo[sl]), int(e_hi[sl]), false, cs);
-        if (int st = elem_down(out_mat, e_lo[sl], e_hi[sl], d->ev_mat[sl], cs)) return st;
+        if (int st = elem_down(out_mat, e_lo[sl], e_hi[sl], d->ev_mat[sl], cs, LULESH_TL_MAT, sl)) return st;
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(d->ev_s2, d->stream2));
@@ -848,7 +876,14 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     CK(cudaMemcpyAsync(d->h_result, m.result, sizeof(StepResult), cudaMemcpyDeviceToHost, d->stream));
     CK(cudaMemcpyAsync(d->h_result + 1, d->slab_result, sizeof(StepResult) * slabs, cudaMemcpyDeviceToHost,
                        d->stream));
+    if (int st = mark(LULESH_TL_END, 0, d->stream)) return st;
     for (cudaStream_t st : {d->stream, d->cstream, d->mstream, d->mstream2}) CK(cudaStreamSynchronize(st));
+    if (d->tl_on) {
+        d->tl_last.n = d->tl_n;
+        for (int k = 0; k < d->tl_n; ++k) CK(cudaEventElapsedTime(&d->tl_last.ms[k], d->tl_ev[0], d->tl_ev[1 + k]));
+        d->tl_last.wall_ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_call).count();
+    }
     if (d->h_result->err != 0) {
         d->err_elem = d->h_result->err_elem;
         return d->h_result->err;
@@ -862,6 +897,20 @@ int lulesh_leapfrog(lulesh_dev* d, lulesh_domain_view* v) {
     v->time->dtcourant = dtc;
     v->time->dthydro = dth;
     d->geo_valid = geo;
+    return LULESH_OK;
+}
+
+int lulesh_leapfrog_timeline(lulesh_dev* d, int32_t on) {
+    if (!d) return LULESH_EINVAL;
+    if (on && !d->tl_ev[0])
+        for (cudaEvent_t& e : d->tl_ev) CK(cudaEventCreate(&e));
+    d->tl_on = on != 0;
+    return LULESH_OK;
+}
+
+int lulesh_leapfrog_timeline_read(const lulesh_dev* d, lulesh_timeline* out) {
+    if (!d || !out) return LULESH_EINVAL;
+    *out = d->tl_last;
     return LULESH_OK;
 }
 

@@ -342,6 +342,33 @@ def test_leapfrog_with_host_changed_coordinates(lulesh, size, node):
     dev_b.close()
 
 
+def test_leapfrog_timeline_marks_and_unchanged_results(lulesh):
+    """lulesh_leapfrog_timeline records the drop-in call's stage boundaries
+    (s=10: 8 slab uploads and force slabs, 4 node ranges, 4 kinematics
+    groups, 8 material slabs, each download) without changing its results:
+    a run with the timeline on equals one with it off bit for bit."""
+    a, b = lulesh.HostDomain(10), lulesh.HostDomain(10)
+    dev_a, dev_b = lulesh.Device(a, "fp64"), lulesh.Device(b, "fp64")
+    dev_a.timeline(True)
+    for _ in range(6):
+        a.time_increment()
+        dev_a.leapfrog()
+        b.time_increment()
+        dev_b.leapfrog()
+    t = dev_a.timeline_read()
+    count = {}
+    for name, _, ms in t["marks"]:
+        count[name] = count.get(name, 0) + 1
+        assert ms >= 0.0
+    assert count == {"upload": 8, "forces": 8, "energy_up": 1, "nodes": 4, "nodes_down": 4, "kinematics": 4,
+                     "kinematics_down": 4, "material": 8, "material_down": 8, "end": 1}
+    assert t["wall_ms"] > 0.0
+    for f in NODE + ELEM:
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
+    dev_a.close()
+    dev_b.close()
+
+
 def test_geometry_hand_offs_between_entry_points(lulesh):
     """The element geometry the double path keeps between phases stays valid
     across the entry points that keep the coordinates (drop-in call, host
